@@ -1,0 +1,43 @@
+"""The oracle restatement against the reference built from its own sources,
+live, on inputs beyond the fixtures.  Skipped where the reference is absent."""
+import numpy as np
+import pytest
+
+from cloth_sim_self_collision_gb300 import scene
+from oracle import oracle as O
+
+
+def test_elements_random(oracle_port, oracle_ref):
+    rng = np.random.default_rng(1234)
+    for _ in range(200):
+        C = rng.uniform(-1, 1, 9)
+        c = C + rng.normal(0, 0.5, 9)
+        a = O.wdwddw_cst(oracle_port, C, c, 0.7, 1.3)
+        b = O.wdwddw_cst(oracle_ref, C, c, 0.7, 1.3)
+        assert a[0] == b[0] and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+        C4 = rng.uniform(-1, 1, 12)
+        c4 = C4 + rng.normal(0, 0.5, 12)
+        a = O.wdwddw_bend(oracle_port, C4, c4, 0.01)
+        b = O.wdwddw_bend(oracle_ref, C4, c4, 0.01)
+        assert a[0] == b[0] and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+@pytest.mark.parametrize("side,steps", [(61, 3), (101, 2)])
+def test_large_sheet_steps(oracle_port, oracle_ref, side, steps):
+    c = scene.square_cloth(side, 2.0, 1.0, sphere_radius=0.25, solver_kind=scene.SOLVER_CG,
+                           tol=1e-6, maxit=1000)
+    a = O.OracleCloth(oracle_port, c)
+    b = O.OracleCloth(oracle_ref, c)
+    assert np.array_equal(a.bvh_nodes(), b.bvh_nodes())
+    for _ in range(steps):
+        assert a.step(1) == b.step(1)
+        assert np.array_equal(a.x, b.x) and np.array_equal(a.v, b.v)
+
+
+def test_batch_instances_topology(oracle_port, oracle_ref):
+    for c in scene.config_batch(count=6):
+        a = O.OracleCloth(oracle_port, c)
+        b = O.OracleCloth(oracle_ref, c)
+        assert np.array_equal(a.bvh_nodes(), b.bvh_nodes())
+        assert a.step(1) == b.step(1)
+        assert np.array_equal(a.x, b.x)
