@@ -1,0 +1,1250 @@
+// api.cu -- the C ABI (include/clothgpu.h): contexts, the device arena of
+// cloths, and the host orchestration of the frame
+// (self_contact_sparse/main.cpp:213-263).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/clothgpu.h"
+#include "kernels.h"
+#include "topology.h"
+
+using namespace cs;
+
+namespace {
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+struct ArgError : std::runtime_error {
+  explicit ArgError(const std::string& s) : std::runtime_error(s) {}
+};
+struct CapacityError : std::runtime_error {
+  explicit CapacityError(const std::string& s) : std::runtime_error(s) {}
+};
+
+#define CK(expr)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (expr);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      throw CudaError(std::string(#expr) + ": " + cudaGetErrorString(e_) + " (" __FILE__ ":" +   \
+                      std::to_string(__LINE__) + ")");                                            \
+  } while (0)
+
+struct Cloth {
+  int id = 0;
+  ClothTopo topo;
+  cs_params prm{};
+  std::vector<double> x, v;  // host copy, authoritative only while the arena is rebuilt
+  cs_stats stats{};
+};
+
+// device allocation with ownership in the context
+struct DevMem {
+  std::vector<void*> ptrs;
+  template <typename T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) throw CudaError(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    ptrs.push_back(p);
+    return (T*)p;
+  }
+  template <typename T>
+  T* upload(const std::vector<T>& h, cudaStream_t s) {
+    T* d = alloc<T>(h.size());
+    if (!h.empty()) CK(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+}  // namespace
+
+struct cs_ctx {
+  int device = 0;
+  int precision = CS_PREC_FP64;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::map<int, std::unique_ptr<Cloth>> cloths;
+  std::vector<int> order;  // arena slot -> cloth id
+  int next_id = 0;
+  bool dirty = true;
+  Arena A;
+  ContactBufs C;
+  DevMem mem, cmem;  // arena / contact buffers
+  // host mirrors of arena offsets
+  std::vector<int> voff, toff, boff, noff, qoff;
+  std::vector<int> solver;  // per slot
+  int* d_list = nullptr;    // scratch list of cloth slots
+  int token = 0;
+  std::vector<InstState> hst;
+  long long launches0 = 0;
+};
+
+namespace {
+
+int slot_of(cs_ctx* c, int id) {
+  for (size_t i = 0; i < c->order.size(); i++)
+    if (c->order[i] == id) return (int)i;
+  throw ArgError("unknown cloth id " + std::to_string(id));
+}
+
+DevParams to_dev(const cs_params& p) {
+  DevParams d;
+  static_assert(sizeof(DevParams) == sizeof(cs_params), "parameter layouts differ");
+  std::memcpy(&d, &p, sizeof(d));
+  return d;
+}
+
+void free_contacts(cs_ctx* c) {
+  c->cmem.release();
+  c->C = ContactBufs();
+}
+
+void alloc_contacts(cs_ctx* c, int pair_cap, int cand_cap) {
+  free_contacts(c);
+  const Arena& A = c->A;
+  ContactBufs& C = c->C;
+  DevMem& m = c->cmem;
+  C.pair_cap = pair_cap;
+  C.cand_cap = cand_cap;
+  C.ce_cap = cand_cap;
+  C.pairs = m.alloc<int2>(pair_cap);
+  C.cand = m.alloc<Cand>(cand_cap);
+  C.cand_sorted = m.alloc<Cand>(cand_cap);
+  C.key_a = m.alloc<unsigned long long>(cand_cap);
+  C.key_b = m.alloc<unsigned long long>(cand_cap);
+  C.idx_a = m.alloc<int>(cand_cap);
+  C.idx_b = m.alloc<int>(cand_cap);
+  C.ce = m.alloc<int>(5 * (size_t)cand_cap);
+  C.ce_inst_lo = m.alloc<int>(A.ni);
+  C.ce_inst_hi = m.alloc<int>(A.ni);
+  C.counters = m.alloc<int>(8);
+  C.level = m.alloc<int>(cand_cap);
+  C.order = m.alloc<int>(cand_cap);
+  C.lev_cnt = m.alloc<int>((size_t)cand_cap + A.ni + 1);
+  C.vmark = m.alloc<int>(A.nv);
+  C.vstamp = m.alloc<int>(A.nv);
+  C.zkey = m.alloc<unsigned long long>(A.nv);
+  C.zkey2 = m.alloc<unsigned long long>(A.nv);
+  C.zrec = m.alloc<double>(9 * (size_t)A.nv);
+  C.cub_bytes = cub_sort_bytes(std::max(cand_cap, A.nv));
+  C.cub_tmp = m.alloc<char>(C.cub_bytes);
+  CK(cudaMemsetAsync(C.vstamp, 0xff, sizeof(int) * (size_t)A.nv, c->stream));
+  CK(cudaMemsetAsync(C.counters, 0, sizeof(int) * 8, c->stream));
+  c->token = 0;
+}
+
+// Rebuilds the device arena from the cloths, keeping their states.
+void rebuild(cs_ctx* c) {
+  // save resident states
+  if (!c->dirty) return;
+  c->mem.release();
+  free_contacts(c);
+  Arena A;
+  const int ni = (int)c->order.size();
+  A.ni = ni;
+  c->voff.assign(ni + 1, 0);
+  c->toff.assign(ni + 1, 0);
+  c->qoff.assign(ni + 1, 0);
+  c->boff.assign(ni + 1, 0);
+  c->noff.assign(ni + 1, 0);
+  c->solver.assign(ni, 0);
+  std::vector<int> eoff(ni + 1, 0), chunk_off(ni + 1, 0);
+  for (int i = 0; i < ni; i++) {
+    const ClothTopo& t = c->cloths[c->order[i]]->topo;
+    c->voff[i + 1] = c->voff[i] + t.np;
+    c->toff[i + 1] = c->toff[i] + t.nt;
+    c->qoff[i + 1] = c->qoff[i] + t.nq;
+    c->boff[i + 1] = c->boff[i] + t.nb;
+    c->noff[i + 1] = c->noff[i] + t.nnode;
+    eoff[i + 1] = eoff[i] + (int)t.edge_uv.size() / 2;
+    chunk_off[i + 1] = chunk_off[i] + (t.np + 255) / 256;
+    c->solver[i] = c->cloths[c->order[i]]->prm.solver_kind;
+  }
+  A.nv = c->voff[ni];
+  A.nt = c->toff[ni];
+  A.nq = c->qoff[ni];
+  A.nb = c->boff[ni];
+  A.nn = c->noff[ni];
+  A.ne = eoff[ni];
+  A.nchunk = chunk_off[ni];
+  const int NV = A.nv, NT = A.nt, NQ = A.nq, NB = A.nb, NN = A.nn;
+  std::vector<double> X0, x, v;
+  std::vector<int> bc, vinst, tri, tinst, quad, qinst, row_ptr, col_idx, dia_split, blk_row;
+  std::vector<int> slot_ptr(1, 0), slot_src, grad_ptr(1, 0), grad_src;
+  std::vector<int> lev_off(1, 0), lev_ptr(1, 0), lev_rows, blev_off(1, 0), blev_ptr(1, 0), blev_rows;
+  std::vector<int> fac_ptr(1, 0), fac_ops;
+  std::vector<int> node, pre, skip, leaf_lo, leaf_hi, depth, prepos(NN), tri_leaf(NT), edge_uv;
+  std::vector<int> chunk_inst, chunk_lo(ni), chunk_hi(ni);
+  std::vector<DevParams> prm;
+  X0.reserve(3 * (size_t)NV);
+  for (int i = 0; i < ni; i++) {
+    const Cloth& cl = *c->cloths[c->order[i]];
+    const ClothTopo& t = cl.topo;
+    const int vo = c->voff[i], to = c->toff[i], qo = c->qoff[i], bo = c->boff[i], no = c->noff[i];
+    prm.push_back(to_dev(cl.prm));
+    X0.insert(X0.end(), t.X0.begin(), t.X0.end());
+    x.insert(x.end(), cl.x.begin(), cl.x.end());
+    v.insert(v.end(), cl.v.begin(), cl.v.end());
+    bc.insert(bc.end(), t.bc.begin(), t.bc.end());
+    vinst.insert(vinst.end(), t.np, i);
+    for (int k : t.tri) tri.push_back(k + vo);
+    tinst.insert(tinst.end(), t.nt, i);
+    for (int k : t.quad) quad.push_back(k + vo);
+    qinst.insert(qinst.end(), t.nq, i);
+    for (int r = 0; r < t.np; r++) {
+      row_ptr.push_back(t.row_ptr[r] + bo);
+      dia_split.push_back(t.dia_split[r] + bo);
+      for (int s = t.row_ptr[r]; s < t.row_ptr[r + 1]; s++) blk_row.push_back(r + vo);
+    }
+    for (int k : t.col_idx) col_idx.push_back(k + vo);
+    for (int k = 0; k < (int)t.edge_uv.size(); k++) edge_uv.push_back(t.edge_uv[k] + vo);
+    for (int k = chunk_off[i]; k < chunk_off[i + 1]; k++) chunk_inst.push_back(i);
+    chunk_lo[i] = chunk_off[i];
+    chunk_hi[i] = chunk_off[i + 1];
+    // BVH
+    for (int n = 0; n < t.nnode; n++) {
+      const int par = t.node[3 * n], c0 = t.node[3 * n + 1], c1 = t.node[3 * n + 2];
+      node.push_back(par < 0 ? -1 : par + no);
+      if (c1 == -1) {
+        node.push_back(c0 + to);
+        node.push_back(-1);
+        tri_leaf[c0 + to] = n + no;
+      } else {
+        node.push_back(c0 + no);
+        node.push_back(c1 + no);
+      }
+      leaf_lo.push_back(t.leaf_lo[n]);
+      leaf_hi.push_back(t.leaf_hi[n]);
+      depth.push_back(t.depth[n]);
+    }
+    for (int k = 0; k < t.nnode; k++) {
+      pre.push_back(t.pre[k] + no);
+      skip.push_back(t.skip[k] + no);
+      prepos[t.pre[k] + no] = k;
+    }
+    // ILU level tables (rows global)
+    if (!t.lev_ptr.empty()) {
+      const int rb = lev_ptr.back();
+      for (size_t l = 1; l < t.lev_ptr.size(); l++) lev_ptr.push_back(rb + t.lev_ptr[l]);
+      for (int r : t.lev_rows) lev_rows.push_back(r + vo);
+      const int rbb = blev_ptr.back();
+      for (size_t l = 1; l < t.blev_ptr.size(); l++) blev_ptr.push_back(rbb + t.blev_ptr[l]);
+      for (int r : t.blev_rows) blev_rows.push_back(r + vo);
+    }
+    lev_off.push_back((int)lev_ptr.size() - 1);
+    blev_off.push_back((int)blev_ptr.size() - 1);
+    const int fb = fac_ptr.back();
+    for (int r = 0; r < t.np; r++) fac_ptr.push_back(fb + (t.fac_ptr.empty() ? 0 : t.fac_ptr[r + 1]));
+    for (size_t k = 0; k < t.fac_ops.size(); k += 3) {
+      fac_ops.push_back(t.fac_ops[k] + bo);
+      fac_ops.push_back(t.fac_ops[k + 1] + bo);
+      fac_ops.push_back(t.fac_ops[k + 2] < 0 ? -1 : t.fac_ops[k + 2] + bo);
+    }
+  }
+  row_ptr.push_back(NB);
+  // slot lists: every cloth's off-diagonal slots, then every cloth's diagonal slots
+  auto glob = [&](int i, int code, int per_tri, int per_quad) {
+    return code >= 0 ? code + c->toff[i] * per_tri : -((-code - 1) + c->qoff[i] * per_quad) - 1;
+  };
+  for (int i = 0; i < ni; i++) {
+    const ClothTopo& t = c->cloths[c->order[i]]->topo;
+    for (int s = 0; s < t.nb; s++) {
+      for (int e = t.slot_ptr[s]; e < t.slot_ptr[s + 1]; e++) slot_src.push_back(glob(i, t.slot_src[e], 9, 16));
+      slot_ptr.push_back((int)slot_src.size());
+    }
+  }
+  for (int i = 0; i < ni; i++) {
+    const ClothTopo& t = c->cloths[c->order[i]]->topo;
+    for (int s = t.nb; s < t.nb + t.np; s++) {
+      for (int e = t.slot_ptr[s]; e < t.slot_ptr[s + 1]; e++) slot_src.push_back(glob(i, t.slot_src[e], 9, 16));
+      slot_ptr.push_back((int)slot_src.size());
+    }
+    for (int r = 0; r < t.np; r++) {
+      for (int e = t.grad_ptr[r]; e < t.grad_ptr[r + 1]; e++) grad_src.push_back(glob(i, t.grad_src[e], 3, 4));
+      grad_ptr.push_back((int)grad_src.size());
+    }
+  }
+  cudaStream_t s = c->stream;
+  DevMem& m = c->mem;
+  std::vector<int> ones(ni, 1);
+  A.active = m.upload(ones, s);
+  A.voff = m.upload(c->voff, s);
+  A.toff = m.upload(c->toff, s);
+  A.qoff = m.upload(c->qoff, s);
+  A.boff = m.upload(c->boff, s);
+  A.noff = m.upload(c->noff, s);
+  A.preoff = A.noff;
+  A.chunk_lo = m.upload(chunk_lo, s);
+  A.chunk_hi = m.upload(chunk_hi, s);
+  A.chunk_inst = m.upload(chunk_inst, s);
+  A.prm = m.upload(prm, s);
+  A.st = m.alloc<InstState>(ni);
+  CK(cudaMemsetAsync(A.st, 0, sizeof(InstState) * (size_t)std::max(ni, 1), s));
+  A.X0 = m.upload(X0, s);
+  A.x = m.upload(x, s);
+  A.v = m.upload(v, s);
+  A.x1 = m.alloc<double>(3 * (size_t)NV);
+  A.v0 = m.alloc<double>(3 * (size_t)NV);
+  A.bc = m.upload(bc, s);
+  A.vinst = m.upload(vinst, s);
+  A.tri = m.upload(tri, s);
+  A.tinst = m.upload(tinst, s);
+  A.quad = m.upload(quad, s);
+  A.qinst = m.upload(qinst, s);
+  A.qK = m.alloc<double>(4 * (size_t)NQ);
+  A.qscale = m.alloc<double>(NQ);
+  A.tri_blk = m.alloc<double>(81 * (size_t)NT);
+  A.tri_grad = m.alloc<double>(9 * (size_t)NT);
+  A.quad_grad = m.alloc<double>(12 * (size_t)NQ);
+  A.row_ptr = m.upload(row_ptr, s);
+  A.col_idx = m.upload(col_idx, s);
+  A.dia_split = m.upload(dia_split, s);
+  A.blk_row = m.upload(blk_row, s);
+  A.slot_ptr = m.upload(slot_ptr, s);
+  A.slot_src = m.upload(slot_src, s);
+  A.grad_ptr = m.upload(grad_ptr, s);
+  A.grad_src = m.upload(grad_src, s);
+  A.vdia = m.alloc<double>(9 * (size_t)NV);
+  A.vcrs = m.alloc<double>(9 * (size_t)NB);
+  A.fdia = m.alloc<double>(9 * (size_t)NV);
+  A.fcrs = m.alloc<double>(9 * (size_t)NB);
+  A.b = m.alloc<double>(3 * (size_t)NV);
+  A.r = m.alloc<double>(3 * (size_t)NV);
+  A.p = m.alloc<double>(3 * (size_t)NV);
+  A.z = m.alloc<double>(3 * (size_t)NV);
+  A.dx = m.alloc<double>(3 * (size_t)NV);
+  CK(cudaMemsetAsync(A.z, 0, sizeof(double) * 3 * (size_t)std::max(NV, 1), s));
+  A.part = m.alloc<double>(2 * (size_t)A.nchunk);
+  A.lev_off = m.upload(lev_off, s);
+  A.lev_ptr = m.upload(lev_ptr, s);
+  A.lev_rows = m.upload(lev_rows, s);
+  A.blev_off = m.upload(blev_off, s);
+  A.blev_ptr = m.upload(blev_ptr, s);
+  A.blev_rows = m.upload(blev_rows, s);
+  A.fac_ptr = m.upload(fac_ptr, s);
+  A.fac_ops = m.upload(fac_ops, s);
+  A.sing = m.alloc<int>(NV);
+  A.node = m.upload(node, s);
+  A.pre = m.upload(pre, s);
+  A.skip = m.upload(skip, s);
+  A.leaf_lo = m.upload(leaf_lo, s);
+  A.leaf_hi = m.upload(leaf_hi, s);
+  A.depth = m.upload(depth, s);
+  A.prepos = m.upload(prepos, s);
+  A.tri_leaf = m.upload(tri_leaf, s);
+  A.refit_cnt = m.alloc<int>(NN);
+  A.box = m.alloc<Box>(NN);
+  A.edge_uv = m.upload(edge_uv, s);
+  A.uf = m.alloc<int>(NV);
+  A.inzone = m.alloc<int>(NV);
+  CK(cudaMemsetAsync(A.inzone, 0, sizeof(int) * (size_t)std::max(NV, 1), s));
+  c->d_list = m.alloc<int>(std::max(ni, 1));
+  c->A = A;
+  if (ni > 0) launch_quad_factors(A, s);
+  alloc_contacts(c, 16 * NT + 4096, 4 * NT + 4096);
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  c->hst.assign(ni, InstState());
+  c->dirty = false;
+}
+
+// copies resident states back to the cloths before the arena changes
+void save_states(cs_ctx* c) {
+  if (c->dirty || c->order.empty()) return;
+  for (size_t i = 0; i < c->order.size(); i++) {
+    Cloth& cl = *c->cloths[c->order[i]];
+    CK(cudaMemcpyAsync(cl.x.data(), c->A.x + 3 * (size_t)c->voff[i], sizeof(double) * cl.x.size(),
+                       cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(cl.v.data(), c->A.v + 3 * (size_t)c->voff[i], sizeof(double) * cl.v.size(),
+                       cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+}
+
+void set_active(cs_ctx* c, const std::vector<int>& act) {
+  CK(cudaMemcpyAsync(c->A.active, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, c->stream));
+}
+
+void pull_states(cs_ctx* c) {
+  c->hst.resize(c->A.ni);
+  CK(cudaMemcpyAsync(c->hst.data(), c->A.st, sizeof(InstState) * (size_t)c->A.ni, cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+}
+
+// ---- implicit step --------------------------------------------------------------
+void assemble(cs_ctx* c) {
+  const Arena& A = c->A;
+  launch_elements(A, true, true, c->stream);
+  launch_slot_reduce(A, c->stream);
+  launch_rhs(A, c->stream);
+}
+
+// CG on the cloths flagged in cg (others must be inactive for the duration)
+void run_cg(cs_ctx* c, const std::vector<int>& cg, double tol, int maxit) {
+  const Arena& A = c->A;
+  set_active(c, cg);
+  int cap = 0;
+  for (int i = 0; i < A.ni; i++)
+    if (cg[i]) cap = std::max(cap, maxit >= 0 ? maxit : c->cloths[c->order[i]]->prm.maxit);
+  launch_cg_init(A, tol, maxit, c->stream);
+  for (int it = 1; it < cap; it++) {
+    launch_cg_iteration(A, it, tol, maxit, c->stream);
+    if (it % 8 == 0) {
+      pull_states(c);
+      bool all = true;
+      for (int i = 0; i < A.ni; i++)
+        if (cg[i] && !c->hst[i].done) all = false;
+      if (all) break;
+    }
+  }
+}
+
+// solves A dx = b for the active cloths with each cloth's own solver
+void solve(cs_ctx* c, const std::vector<int>& act) {
+  const Arena& A = c->A;
+  std::vector<int> ilu, cg(A.ni, 0);
+  bool any_cg = false;
+  for (int i = 0; i < A.ni; i++) {
+    if (!act[i]) continue;
+    if (c->solver[i] == CS_SOLVER_CG) {
+      cg[i] = 1;
+      any_cg = true;
+    } else {
+      ilu.push_back(i);
+    }
+  }
+  if (!ilu.empty()) {
+    CK(cudaMemcpyAsync(c->d_list, ilu.data(), sizeof(int) * ilu.size(), cudaMemcpyHostToDevice, c->stream));
+    launch_ilu_factor(A, c->d_list, (int)ilu.size(), c->stream);
+    launch_pcg(A, c->d_list, (int)ilu.size(), -1.0, -1, c->stream);
+  }
+  if (any_cg) run_cg(c, cg, -1.0, -1);
+  set_active(c, act);
+}
+
+void implicit(cs_ctx* c, const std::vector<int>& act) {
+  set_active(c, act);
+  assemble(c);
+  solve(c, act);
+  launch_finish_implicit(c->A, c->stream);
+}
+
+// ---- contacts ---------------------------------------------------------------------
+// detection for the active cloths; returns the total number of contacts and
+// leaves per-cloth counts in c->hst
+int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_override) {
+  cudaStream_t s = c->stream;
+  launch_refit(c->A, ccd, xs, vs, delta_override, s);
+  int cnt[4];
+  for (int attempt = 0;; attempt++) {
+    CK(cudaMemsetAsync(c->C.counters, 0, sizeof(int) * 4, s));
+    launch_traverse(c->A, c->C, s);
+    CK(cudaMemcpyAsync(cnt, c->C.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (!cnt[3]) break;
+    if (attempt > 4) throw CapacityError("broad-phase pair buffer keeps overflowing");
+    alloc_contacts(c, (int)std::min<long long>(2LL * cnt[0] + 4096, 0x7fffffffLL / 2), c->C.cand_cap);
+  }
+  const int npairs = cnt[0];
+  for (int attempt = 0;; attempt++) {
+    CK(cudaMemsetAsync(c->C.counters + 1, 0, sizeof(int) * 3, s));
+    launch_narrow(c->A, c->C, ccd, xs, vs, delta_override, npairs, s);
+    CK(cudaMemcpyAsync(cnt, c->C.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (!cnt[3]) break;
+    if (attempt > 4) throw CapacityError("contact candidate buffer keeps overflowing");
+    const int pairs_keep = c->C.pair_cap;
+    // the pair list must survive the regrow: recompute it after growing
+    alloc_contacts(c, pairs_keep, (int)std::min<long long>(2LL * cnt[1] + 4096, 0x7fffffffLL / 8));
+    CK(cudaMemsetAsync(c->C.counters, 0, sizeof(int) * 4, s));
+    launch_traverse(c->A, c->C, s);
+  }
+  const int ncand = cnt[1];
+  sort_dedupe(c->A, c->C, ncand, s);
+  CK(cudaGetLastError());
+  int total = 0;
+  CK(cudaMemcpyAsync(&total, c->C.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  pull_states(c);
+  return total;
+}
+
+void impulses(cs_ctx* c, int ccd, const double* xs, double* vs) {
+  c->token++;
+  launch_impulses(c->A, c->C, ccd, xs, vs, c->token, c->stream);
+}
+
+// GetIntermidiateVelocityContactResolved (self_collision_cloth.cpp:355-456) for
+// the cloths in act, positions A.x1, velocities A.v in place; returns the
+// impulse-applied flag per cloth
+std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
+  const Arena& A = c->A;
+  const int ni = A.ni;
+  std::vector<int> applied(ni, 0), phase = act;
+  for (int i = 0; i < ni; i++)
+    if (act[i]) {
+      cs_stats& st = c->cloths[c->order[i]]->stats;
+      const int it = st.solver_iterations, sing = st.ilu_singular;
+      const double conv = st.solver_conv;
+      std::memset(&st, 0, sizeof(st));
+      st.solver_iterations = it;
+      st.ilu_singular = sing;
+      st.solver_conv = conv;
+    }
+  set_active(c, phase);
+  detect(c, 0, A.x1, nullptr, -1.0);
+  for (int i = 0; i < ni; i++)
+    if (act[i]) {
+      c->cloths[c->order[i]]->stats.n_prx = c->hst[i].n_contacts;
+      applied[i] = c->hst[i].n_contacts > 0;
+    }
+  impulses(c, 0, A.x1, A.v);
+  for (int it = 0; it < 5; it++) {
+    bool any = false;
+    for (int i = 0; i < ni; i++) any |= phase[i] != 0;
+    if (!any) break;
+    set_active(c, phase);
+    detect(c, 1, A.x1, A.v, -1.0);
+    for (int i = 0; i < ni; i++) {
+      if (!phase[i]) continue;
+      cs_stats& st = c->cloths[c->order[i]]->stats;
+      st.n_ccd[it] = c->hst[i].n_contacts;
+      st.n_ccd_passes = it + 1;
+      if (c->hst[i].n_contacts == 0)
+        phase[i] = 0;
+      else
+        applied[i] = 1;
+    }
+    set_active(c, phase);
+    impulses(c, 1, A.x1, A.v);
+  }
+  bool any = false;
+  for (int i = 0; i < ni; i++) any |= phase[i] != 0;
+  if (any) {
+    set_active(c, phase);
+    CK(cudaMemcpyAsync(A.v0, A.v, sizeof(double) * 3 * (size_t)A.nv, cudaMemcpyDeviceToDevice, c->stream));
+    launch_riz_reset(A, c->stream);
+    for (int it = 0; it < 100; it++) {
+      bool more = false;
+      for (int i = 0; i < ni; i++) more |= phase[i] != 0;
+      if (!more) break;
+      set_active(c, phase);
+      detect(c, 1, A.x1, A.v, -1.0);
+      launch_riz_count(A, c->stream);
+      pull_states(c);
+      int nce = 0;
+      CK(cudaMemcpyAsync(&nce, c->C.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      for (int i = 0; i < ni; i++) {
+        if (!phase[i]) continue;
+        cs_stats& st = c->cloths[c->order[i]]->stats;
+        const int n = c->hst[i].n_contacts;
+        st.n_riz_passes++;
+        st.n_riz_last = n;
+        st.n_riz_total += n;
+        st.riz_nodes = c->hst[i].riz_nodes;
+        if (n == 0) phase[i] = 0;
+      }
+      set_active(c, phase);
+      bool work = false;
+      for (int i = 0; i < ni; i++) work |= phase[i] != 0;
+      if (!work) break;
+      launch_riz_add(A, c->C, nce, c->stream);
+      riz_apply(A, c->C, A.x1, A.v, A.v0, c->stream);
+    }
+  }
+  for (int i = 0; i < ni; i++)
+    if (act[i]) c->cloths[c->order[i]]->stats.impulse_applied = applied[i];
+  set_active(c, act);
+  return applied;
+}
+
+void update_velocity(cs_ctx* c, const std::vector<int>& act) {
+  set_active(c, act);
+  launch_elements(c->A, false, true, c->stream);
+  launch_update_velocity(c->A, c->stream);
+}
+
+// one frame for the cloths in act (StepTime, self_contact_sparse/main.cpp:213-263)
+void frame(cs_ctx* c, const std::vector<int>& act) {
+  const Arena& A = c->A;
+  CK(cudaMemcpyAsync(A.x1, A.x, sizeof(double) * 3 * (size_t)A.nv, cudaMemcpyDeviceToDevice, c->stream));
+  implicit(c, act);
+  pull_states(c);
+  for (int i = 0; i < A.ni; i++)
+    if (act[i]) {
+      cs_stats& st = c->cloths[c->order[i]]->stats;
+      st.solver_iterations = c->hst[i].solver_iterations;
+      st.solver_conv = c->hst[i].solver_conv;
+      st.ilu_singular = c->solver[i] == CS_SOLVER_ILU_PCG ? c->hst[i].ilu_singular : 0;
+    }
+  std::vector<int> applied = resolve(c, act);
+  bool any = false;
+  for (int i = 0; i < A.ni; i++) any |= applied[i] != 0;
+  if (any) {
+    set_active(c, applied);
+    launch_reintegrate(A, c->stream);
+    update_velocity(c, applied);
+  }
+  set_active(c, act);
+}
+
+std::vector<int> only(cs_ctx* c, int slot) {
+  std::vector<int> a(c->A.ni, 0);
+  a[slot] = 1;
+  return a;
+}
+
+void up(cs_ctx* c, double* dst, const double* src, size_t n) {
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+}
+void down(cs_ctx* c, double* dst, const double* src, size_t n) {
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+}
+
+template <typename F>
+int guarded(cs_ctx* c, F&& f) {
+  if (!c) return CS_ERR_ARG;
+  try {
+    f();
+    return CS_OK;
+  } catch (const ArgError& e) {
+    c->err = e.what();
+    return CS_ERR_ARG;
+  } catch (const CapacityError& e) {
+    c->err = e.what();
+    return CS_ERR_CAPACITY;
+  } catch (const CudaError& e) {
+    c->err = e.what();
+    return std::string(e.what()).find("out of memory") != std::string::npos ? CS_ERR_OOM : CS_ERR_CUDA;
+  } catch (const std::exception& e) {
+    c->err = e.what();
+    return CS_ERR_ARG;
+  }
+}
+
+Cloth& cloth_at(cs_ctx* c, int id) {
+  auto it = c->cloths.find(id);
+  if (it == c->cloths.end()) throw ArgError("unknown cloth id " + std::to_string(id));
+  return *it->second;
+}
+
+void ensure(cs_ctx* c) {
+  if (c->dirty) rebuild(c);
+  CK(cudaSetDevice(c->device));
+}
+
+}  // namespace
+
+extern "C" {
+
+int cs_create(int device, int precision, cs_ctx** out) {
+  if (!out) return CS_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CS_ERR_NO_DEVICE;
+  if (device < 0 || device >= n) return CS_ERR_ARG;
+  if (precision != CS_PREC_FP64 && precision != CS_PREC_MIXED) return CS_ERR_ARG;
+  cs_ctx* c = new cs_ctx();
+  c->device = device;
+  c->precision = precision;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return CS_ERR_CUDA;
+  }
+  c->launches0 = g_launches;
+  *out = c;
+  return CS_OK;
+}
+
+void cs_destroy(cs_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->mem.release();
+  c->cmem.release();
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* cs_last_error(const cs_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int cs_set_precision(cs_ctx* c, int precision) {
+  return guarded(c, [&] {
+    if (precision != CS_PREC_FP64 && precision != CS_PREC_MIXED) throw ArgError("unknown precision");
+    c->precision = precision;
+  });
+}
+
+int cs_synchronize(cs_ctx* c) {
+  return guarded(c, [&] { CK(cudaStreamSynchronize(c->stream)); });
+}
+
+int cs_add_cloth(cs_ctx* c, int np, const double* X0, const int* bc, int nt, const int* tri, int nq,
+                 const int* quad, const cs_params* prm, int* id_out) {
+  return guarded(c, [&] {
+    if (np <= 0 || nt <= 0 || nq < 0 || !X0 || !tri || (nq > 0 && !quad) || !prm)
+      throw ArgError("cs_add_cloth: bad sizes or null arrays");
+    if (prm->solver_kind != CS_SOLVER_ILU_PCG && prm->solver_kind != CS_SOLVER_CG)
+      throw ArgError("cs_add_cloth: unknown solver");
+    if (prm->obstacle_kind < 0 || prm->obstacle_kind > 3) throw ArgError("cs_add_cloth: unknown obstacle");
+    std::unique_ptr<Cloth> cl(new Cloth());
+    std::vector<int> bcv(np, 0);
+    if (bc) bcv.assign(bc, bc + np);
+    build_topology(cl->topo, np, X0, bcv.data(), nt, tri, nq, quad, prm->solver_kind == CS_SOLVER_ILU_PCG);
+    cl->prm = *prm;
+    cl->x.assign(X0, X0 + 3 * (size_t)np);
+    cl->v.assign(3 * (size_t)np, 0.0);
+    save_states(c);
+    cl->id = c->next_id++;
+    c->order.push_back(cl->id);
+    if (id_out) *id_out = cl->id;
+    c->cloths[cl->id] = std::move(cl);
+    c->dirty = true;
+  });
+}
+
+int cs_remove_cloth(cs_ctx* c, int id) {
+  return guarded(c, [&] {
+    cloth_at(c, id);
+    save_states(c);
+    c->order.erase(std::find(c->order.begin(), c->order.end(), id));
+    c->cloths.erase(id);
+    c->dirty = true;
+  });
+}
+
+int cs_num_cloths(const cs_ctx* c) { return c ? (int)c->order.size() : 0; }
+
+int cs_set_params(cs_ctx* c, int id, const cs_params* prm) {
+  return guarded(c, [&] {
+    if (!prm) throw ArgError("null params");
+    Cloth& cl = cloth_at(c, id);
+    if (prm->solver_kind != cl.prm.solver_kind) {
+      // the ILU schedule is part of the topology
+      save_states(c);
+      build_topology(cl.topo, cl.topo.np, cl.topo.X0.data(), cl.topo.bc.data(), cl.topo.nt, cl.topo.tri.data(),
+                     cl.topo.nq, cl.topo.quad.data(), prm->solver_kind == CS_SOLVER_ILU_PCG);
+      cl.prm = *prm;
+      c->dirty = true;
+      return;
+    }
+    cl.prm = *prm;
+    if (!c->dirty) {
+      const DevParams d = to_dev(*prm);
+      CK(cudaMemcpyAsync(c->A.prm + slot_of(c, id), &d, sizeof(d), cudaMemcpyHostToDevice, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      launch_quad_factors(c->A, c->stream);  // bending stiffness may have changed
+    }
+  });
+}
+
+int cs_set_state(cs_ctx* c, int id, const double* x, const double* v) {
+  return guarded(c, [&] {
+    Cloth& cl = cloth_at(c, id);
+    if (c->dirty) {
+      if (x) cl.x.assign(x, x + cl.x.size());
+      if (v) cl.v.assign(v, v + cl.v.size());
+      return;
+    }
+    const int i = slot_of(c, id);
+    if (x) up(c, c->A.x + 3 * (size_t)c->voff[i], x, cl.x.size());
+    if (v) up(c, c->A.v + 3 * (size_t)c->voff[i], v, cl.v.size());
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_get_state(cs_ctx* c, int id, double* x, double* v) {
+  return guarded(c, [&] {
+    Cloth& cl = cloth_at(c, id);
+    if (c->dirty) {
+      if (x) std::memcpy(x, cl.x.data(), sizeof(double) * cl.x.size());
+      if (v) std::memcpy(v, cl.v.data(), sizeof(double) * cl.v.size());
+      return;
+    }
+    const int i = slot_of(c, id);
+    if (x) down(c, x, c->A.x + 3 * (size_t)c->voff[i], cl.x.size());
+    if (v) down(c, v, c->A.v + 3 * (size_t)c->voff[i], cl.v.size());
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_get_stats(cs_ctx* c, int id, cs_stats* st) {
+  return guarded(c, [&] {
+    if (!st) throw ArgError("null stats");
+    *st = cloth_at(c, id).stats;
+  });
+}
+
+int cs_step(cs_ctx* c, int nsteps) {
+  return guarded(c, [&] {
+    if (nsteps < 0) throw ArgError("negative step count");
+    ensure(c);
+    if (c->A.ni == 0) return;
+    if (c->precision != CS_PREC_FP64) throw ArgError("mixed precision is not available in this build");
+    std::vector<int> all(c->A.ni, 1);
+    for (int k = 0; k < nsteps; k++) frame(c, all);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+  });
+}
+
+int cs_implicit_step(cs_ctx* c, int id, double* x, double* v, cs_stats* st) {
+  return guarded(c, [&] {
+    if (!x || !v) throw ArgError("null state");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const size_t n = 3 * (size_t)c->cloths[id]->topo.np;
+    up(c, c->A.x + 3 * (size_t)c->voff[i], x, n);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, n);
+    implicit(c, only(c, i));
+    pull_states(c);
+    down(c, x, c->A.x + 3 * (size_t)c->voff[i], n);
+    down(c, v, c->A.v + 3 * (size_t)c->voff[i], n);
+    CK(cudaStreamSynchronize(c->stream));
+    if (st) {
+      std::memset(st, 0, sizeof(*st));
+      st->solver_iterations = c->hst[i].solver_iterations;
+      st->solver_conv = c->hst[i].solver_conv;
+      st->ilu_singular = c->solver[i] == CS_SOLVER_ILU_PCG ? c->hst[i].ilu_singular : 0;
+    }
+  });
+}
+
+int cs_resolve_contacts(cs_ctx* c, int id, const double* x1, double* v, cs_stats* st) {
+  return guarded(c, [&] {
+    if (!x1 || !v) throw ArgError("null state");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const size_t n = 3 * (size_t)c->cloths[id]->topo.np;
+    up(c, c->A.x1 + 3 * (size_t)c->voff[i], x1, n);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, n);
+    resolve(c, only(c, i));
+    down(c, v, c->A.v + 3 * (size_t)c->voff[i], n);
+    CK(cudaStreamSynchronize(c->stream));
+    if (st) *st = c->cloths[id]->stats;
+  });
+}
+
+int cs_update_velocity(cs_ctx* c, int id, const double* x, double* v) {
+  return guarded(c, [&] {
+    if (!x || !v) throw ArgError("null state");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const size_t n = 3 * (size_t)c->cloths[id]->topo.np;
+    up(c, c->A.x + 3 * (size_t)c->voff[i], x, n);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, n);
+    update_velocity(c, only(c, i));
+    down(c, v, c->A.v + 3 * (size_t)c->voff[i], n);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_assemble(cs_ctx* c, int id, const double* x, const double* v, double* vdia, double* vcrs, double* b) {
+  return guarded(c, [&] {
+    if (!x || !v) throw ArgError("null state");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    up(c, c->A.x + 3 * (size_t)c->voff[i], x, 3 * (size_t)t.np);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, 3 * (size_t)t.np);
+    set_active(c, only(c, i));
+    assemble(c);
+    if (vdia) down(c, vdia, c->A.vdia + 9 * (size_t)c->voff[i], 9 * (size_t)t.np);
+    if (vcrs) down(c, vcrs, c->A.vcrs + 9 * (size_t)c->boff[i], 9 * (size_t)t.nb);
+    if (b) down(c, b, c->A.b + 3 * (size_t)c->voff[i], 3 * (size_t)t.np);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_pattern(cs_ctx* c, int id, int* nb, int* row_ptr, int* col_idx) {
+  return guarded(c, [&] {
+    const ClothTopo& t = cloth_at(c, id).topo;
+    if (nb) *nb = t.nb;
+    if (row_ptr) std::memcpy(row_ptr, t.row_ptr.data(), sizeof(int) * t.row_ptr.size());
+    if (col_idx) std::memcpy(col_idx, t.col_idx.data(), sizeof(int) * t.col_idx.size());
+  });
+}
+
+int cs_ilu_factor(cs_ctx* c, int id, double* fdia, double* fcrs, int* nsing) {
+  return guarded(c, [&] {
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    if (t.lev_ptr.empty()) throw ArgError("cloth was added without the ILU(0) solver");
+    CK(cudaMemcpyAsync(c->d_list, &i, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    launch_ilu_factor(c->A, c->d_list, 1, c->stream);
+    if (fdia) down(c, fdia, c->A.fdia + 9 * (size_t)c->voff[i], 9 * (size_t)t.np);
+    if (fcrs) down(c, fcrs, c->A.fcrs + 9 * (size_t)c->boff[i], 9 * (size_t)t.nb);
+    pull_states(c);
+    if (nsing) *nsing = c->hst[i].ilu_singular;
+  });
+}
+
+int cs_solve_pcg(cs_ctx* c, int id, const double* b, double tol, int maxit, double* x, double* conv, int* iter) {
+  return guarded(c, [&] {
+    if (!b || !x) throw ArgError("null vector");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    if (t.lev_ptr.empty()) throw ArgError("cloth was added without the ILU(0) solver");
+    up(c, c->A.b + 3 * (size_t)c->voff[i], b, 3 * (size_t)t.np);
+    CK(cudaMemcpyAsync(c->d_list, &i, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    launch_pcg(c->A, c->d_list, 1, tol, maxit, c->stream);
+    down(c, x, c->A.dx + 3 * (size_t)c->voff[i], 3 * (size_t)t.np);
+    pull_states(c);
+    if (conv) *conv = c->hst[i].solver_conv;
+    if (iter) *iter = c->hst[i].solver_iterations;
+  });
+}
+
+int cs_solve_cg(cs_ctx* c, int id, const double* b, double tol, int maxit, double* x, double* conv, int* iter) {
+  return guarded(c, [&] {
+    if (!b || !x) throw ArgError("null vector");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    up(c, c->A.b + 3 * (size_t)c->voff[i], b, 3 * (size_t)t.np);
+    run_cg(c, only(c, i), tol, maxit);
+    down(c, x, c->A.dx + 3 * (size_t)c->voff[i], 3 * (size_t)t.np);
+    pull_states(c);
+    if (conv) *conv = c->hst[i].solver_conv;
+    if (iter) *iter = c->hst[i].solver_iterations;
+  });
+}
+
+int cs_spmv(cs_ctx* c, int id, const double* x, double* y) {
+  return guarded(c, [&] {
+    if (!x || !y) throw ArgError("null vector");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const size_t n = 3 * (size_t)c->cloths[id]->topo.np;
+    up(c, c->A.p + 3 * (size_t)c->voff[i], x, n);
+    CK(cudaMemsetAsync(c->A.z, 0, sizeof(double) * 3 * (size_t)c->A.nv, c->stream));
+    launch_spmv(c->A, c->A.p, c->A.z, c->stream);
+    down(c, y, c->A.z + 3 * (size_t)c->voff[i], n);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_bvh_nodes(cs_ctx* c, int id, int* nnode, int* nodes) {
+  return guarded(c, [&] {
+    const ClothTopo& t = cloth_at(c, id).topo;
+    if (nnode) *nnode = t.nnode;
+    if (nodes) std::memcpy(nodes, t.node.data(), sizeof(int) * t.node.size());
+  });
+}
+
+static void boxes_out(cs_ctx* c, int i, int nnode, double* boxes) {
+  std::vector<Box> hb(nnode);
+  CK(cudaMemcpyAsync(hb.data(), c->A.box + c->noff[i], sizeof(Box) * nnode, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int n = 0; n < nnode; n++) {
+    for (int k = 0; k < 3; k++) {
+      boxes[7 * n + 2 * k] = hb[n].lo[k];
+      boxes[7 * n + 2 * k + 1] = hb[n].hi[k];
+    }
+    boxes[7 * n + 6] = hb[n].full ? 1.0 : 0.0;
+  }
+}
+
+int cs_refit_prx(cs_ctx* c, int id, const double* x, double delta, double* boxes) {
+  return guarded(c, [&] {
+    if (!x) throw ArgError("null positions");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    up(c, c->A.x1 + 3 * (size_t)c->voff[i], x, 3 * (size_t)t.np);
+    set_active(c, only(c, i));
+    launch_refit(c->A, 0, c->A.x1, nullptr, delta, c->stream);
+    if (boxes) boxes_out(c, i, t.nnode, boxes);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+// runs f with the cloth's dt replaced (the CCD stages take dt as an argument)
+extern "C++" template <typename F>
+void with_dt(cs_ctx* c, int i, int id, double dt, F&& f) {
+  cs_params p = c->cloths[id]->prm;
+  p.dt = dt;
+  DevParams d = to_dev(p), d0 = to_dev(c->cloths[id]->prm);
+  CK(cudaMemcpyAsync(c->A.prm + i, &d, sizeof(d), cudaMemcpyHostToDevice, c->stream));
+  f();
+  CK(cudaMemcpyAsync(c->A.prm + i, &d0, sizeof(d0), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+}
+
+int cs_refit_ccd(cs_ctx* c, int id, const double* x, const double* v, double dt, double* boxes) {
+  return guarded(c, [&] {
+    if (!x || !v) throw ArgError("null state");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    up(c, c->A.x1 + 3 * (size_t)c->voff[i], x, 3 * (size_t)t.np);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, 3 * (size_t)t.np);
+    set_active(c, only(c, i));
+    with_dt(c, i, id, dt, [&] { launch_refit(c->A, 1, c->A.x1, c->A.v, -1.0, c->stream); });
+    if (boxes) boxes_out(c, i, t.nnode, boxes);
+  });
+}
+
+static void contacts_out(cs_ctx* c, int i, int total, int* out, int cap, int* n) {
+  const int cnt = c->hst[i].n_contacts;
+  if (n) *n = cnt;
+  if (!out) return;
+  int lo = 0;
+  CK(cudaMemcpyAsync(&lo, c->C.ce_inst_lo + i, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const int m = std::min(cnt, cap);
+  std::vector<int> h(5 * (size_t)std::max(m, 1));
+  if (m > 0)
+    CK(cudaMemcpyAsync(h.data(), c->C.ce + 5 * (size_t)lo, sizeof(int) * 5 * (size_t)m, cudaMemcpyDeviceToHost,
+                       c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const int vo = c->voff[i];
+  for (int e = 0; e < m; e++) {
+    out[5 * e] = h[5 * e];
+    for (int k = 1; k < 5; k++) out[5 * e + k] = h[5 * e + k] - vo;
+  }
+  (void)total;
+  if (cnt > cap) throw CapacityError("contact output buffer too small");
+}
+
+int cs_contacts_prx(cs_ctx* c, int id, const double* x, double delta, int* out, int cap, int* n) {
+  return guarded(c, [&] {
+    if (!x) throw ArgError("null positions");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    up(c, c->A.x1 + 3 * (size_t)c->voff[i], x, 3 * (size_t)t.np);
+    set_active(c, only(c, i));
+    const int total = detect(c, 0, c->A.x1, nullptr, delta);
+    contacts_out(c, i, total, out, cap, n);
+  });
+}
+
+int cs_contacts_ccd(cs_ctx* c, int id, const double* x, const double* v, double dt, double delta, int* out, int cap,
+                    int* n) {
+  return guarded(c, [&] {
+    if (!x || !v) throw ArgError("null state");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    up(c, c->A.x1 + 3 * (size_t)c->voff[i], x, 3 * (size_t)t.np);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, 3 * (size_t)t.np);
+    set_active(c, only(c, i));
+    int total = 0;
+    with_dt(c, i, id, dt, [&] { total = detect(c, 1, c->A.x1, c->A.v, delta); });
+    contacts_out(c, i, total, out, cap, n);
+  });
+}
+
+// uploads a host contact list (cloth-local ids) as the cloth's contact segment
+static void contacts_in(cs_ctx* c, int i, const int* ce, int n) {
+  if (n > c->C.ce_cap) alloc_contacts(c, c->C.pair_cap, n + 4096);
+  std::vector<int> h(5 * (size_t)std::max(n, 1));
+  const int vo = c->voff[i];
+  for (int e = 0; e < n; e++) {
+    h[5 * e] = ce[5 * e];
+    for (int k = 1; k < 5; k++) h[5 * e + k] = ce[5 * e + k] + vo;
+  }
+  if (n > 0) CK(cudaMemcpyAsync(c->C.ce, h.data(), sizeof(int) * 5 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  std::vector<int> lo(c->A.ni, 0), hi(c->A.ni, 0);
+  hi[i] = n;
+  CK(cudaMemcpyAsync(c->C.ce_inst_lo, lo.data(), sizeof(int) * lo.size(), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->C.ce_inst_hi, hi.data(), sizeof(int) * hi.size(), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+}
+
+static int impulse_api(cs_ctx* c, int id, const double* x, double* v, const int* ce, int n, int ccd) {
+  return guarded(c, [&] {
+    if (!x || !v || (n > 0 && !ce) || n < 0) throw ArgError("bad arguments");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const size_t nd = 3 * (size_t)c->cloths[id]->topo.np;
+    up(c, c->A.x1 + 3 * (size_t)c->voff[i], x, nd);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, nd);
+    set_active(c, only(c, i));
+    contacts_in(c, i, ce, n);
+    impulses(c, ccd, c->A.x1, c->A.v);
+    down(c, v, c->A.v + 3 * (size_t)c->voff[i], nd);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_impulse_prx(cs_ctx* c, int id, const double* x, double* v, const int* ce, int n) {
+  return impulse_api(c, id, x, v, ce, n, 0);
+}
+int cs_impulse_ccd(cs_ctx* c, int id, const double* x, double* v, const int* ce, int n) {
+  return impulse_api(c, id, x, v, ce, n, 1);
+}
+
+int cs_riz_reset(cs_ctx* c, int id) {
+  return guarded(c, [&] {
+    ensure(c);
+    set_active(c, only(c, slot_of(c, id)));
+    launch_riz_reset(c->A, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_riz_add(cs_ctx* c, int id, const int* ce, int n) {
+  return guarded(c, [&] {
+    if ((n > 0 && !ce) || n < 0) throw ArgError("bad arguments");
+    ensure(c);
+    const int i = slot_of(c, id);
+    set_active(c, only(c, i));
+    contacts_in(c, i, ce, n);
+    launch_riz_add(c->A, c->C, n, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_riz_zones(cs_ctx* c, int id, int* zone_of, int* nzone) {
+  return guarded(c, [&] {
+    ensure(c);
+    const int i = slot_of(c, id);
+    const int np = c->cloths[id]->topo.np;
+    set_active(c, only(c, i));
+    riz_count_zones(c->A, c->C, c->C.idx_a, c->stream);  // labels into scratch (needs nv ints)
+    std::vector<int> lab(c->A.nv);
+    CK(cudaMemcpyAsync(lab.data(), c->C.idx_a, sizeof(int) * (size_t)c->A.nv, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::map<int, int> ids;
+    for (int v = 0; v < np; v++) {
+      const int r = lab[c->voff[i] + v];
+      int z = -1;
+      if (r >= 0) {
+        auto it = ids.find(r);
+        if (it == ids.end()) it = ids.emplace(r, (int)ids.size()).first;
+        z = it->second;
+      }
+      if (zone_of) zone_of[v] = z;
+    }
+    if (nzone) *nzone = (int)ids.size();
+  });
+}
+
+int cs_riz_apply(cs_ctx* c, int id, const double* x, double* v, const double* v0) {
+  return guarded(c, [&] {
+    if (!x || !v || !v0) throw ArgError("null state");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const size_t nd = 3 * (size_t)c->cloths[id]->topo.np;
+    up(c, c->A.x1 + 3 * (size_t)c->voff[i], x, nd);
+    up(c, c->A.v + 3 * (size_t)c->voff[i], v, nd);
+    up(c, c->A.v0 + 3 * (size_t)c->voff[i], v0, nd);
+    set_active(c, only(c, i));
+    riz_apply(c->A, c->C, c->A.x1, c->A.v, c->A.v0, c->stream);
+    down(c, v, c->A.v + 3 * (size_t)c->voff[i], nd);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+extern "C++" template <typename F>
+int element_batch(cs_ctx* c, int n, std::initializer_list<std::pair<const double*, size_t>> ins,
+                         std::initializer_list<std::pair<double*, size_t>> outs, F&& launch) {
+  return guarded(c, [&] {
+    if (n < 0) throw ArgError("negative count");
+    if (n == 0) return;
+    CK(cudaSetDevice(c->device));
+    DevMem tmp;
+    std::vector<double*> din, dout;
+    try {
+      for (auto& p : ins) {
+        if (!p.first) throw ArgError("null input");
+        double* d = tmp.alloc<double>(p.second * n);
+        CK(cudaMemcpyAsync(d, p.first, sizeof(double) * p.second * n, cudaMemcpyHostToDevice, c->stream));
+        din.push_back(d);
+      }
+      for (auto& p : outs) dout.push_back(tmp.alloc<double>(p.second * n));
+      launch(din, dout);
+      size_t k = 0;
+      for (auto& p : outs) {
+        if (p.first)
+          CK(cudaMemcpyAsync(p.first, dout[k], sizeof(double) * p.second * n, cudaMemcpyDeviceToHost, c->stream));
+        k++;
+      }
+      CK(cudaStreamSynchronize(c->stream));
+    } catch (...) {
+      cudaStreamSynchronize(c->stream);
+      tmp.release();
+      throw;
+    }
+    tmp.release();
+  });
+}
+
+int cs_element_cst(cs_ctx* c, int n, const double* C, const double* cc, double lambda, double myu, double* W,
+                   double* dW, double* ddW) {
+  return element_batch(c, n, {{C, 9}, {cc, 9}}, {{W, 1}, {dW, 9}, {ddW, 81}},
+                       [&](std::vector<double*>& i, std::vector<double*>& o) {
+                         launch_element_batch_cst(n, i[0], i[1], lambda, myu, o[0], o[1], o[2], c->stream);
+                       });
+}
+
+int cs_element_bend(cs_ctx* c, int n, const double* C, const double* cc, double stiff, double* W, double* dW,
+                    double* ddW) {
+  return element_batch(c, n, {{C, 12}, {cc, 12}}, {{W, 1}, {dW, 12}, {ddW, 144}},
+                       [&](std::vector<double*>& i, std::vector<double*>& o) {
+                         launch_element_batch_bend(n, i[0], i[1], stiff, o[0], o[1], o[2], c->stream);
+                       });
+}
+
+int cs_element_contact(cs_ctx* c, int n, const double* cc, const cs_params* prm, double* W, double* dW,
+                       double* ddW) {
+  if (!prm) return CS_ERR_ARG;
+  const DevParams d = to_dev(*prm);
+  return element_batch(c, n, {{cc, 3}}, {{W, 1}, {dW, 3}, {ddW, 9}},
+                       [&](std::vector<double*>& i, std::vector<double*>& o) {
+                         launch_element_batch_contact(n, i[0], &d, o[0], o[1], o[2], c->stream);
+                       });
+}
+
+long long cs_launch_count(const cs_ctx* c) { return c ? g_launches - c->launches0 : 0; }
+
+int cs_build_bvh(int np, const double* X, int nt, const int* tri, int* nodes, int cap, int* nnode) {
+  if (np <= 0 || nt <= 0 || !X || !tri) return CS_ERR_ARG;
+  try {
+    ClothTopo t;
+    std::vector<int> bc(np, 0);
+    build_topology(t, np, X, bc.data(), nt, tri, 0, nullptr, false);
+    if (nnode) *nnode = t.nnode;
+    if (!nodes) return CS_OK;
+    if ((long long)cap < 3LL * t.nnode) return CS_ERR_CAPACITY;
+    std::memcpy(nodes, t.node.data(), sizeof(int) * t.node.size());
+    return CS_OK;
+  } catch (...) {
+    return CS_ERR_ARG;
+  }
+}
+
+int cs_build_pattern(int np, int nq, const int* quad, int* row_ptr, int* col_idx, int cap, int* nb) {
+  if (np <= 0 || nq < 0 || (nq > 0 && !quad)) return CS_ERR_ARG;
+  try {
+    ClothTopo t;
+    build_pattern_only(t, np, nq, quad);
+    if (nb) *nb = t.nb;
+    if (row_ptr) std::memcpy(row_ptr, t.row_ptr.data(), sizeof(int) * t.row_ptr.size());
+    if (!col_idx) return CS_OK;
+    if (cap < t.nb) return CS_ERR_CAPACITY;
+    std::memcpy(col_idx, t.col_idx.data(), sizeof(int) * t.col_idx.size());
+    return CS_OK;
+  } catch (...) {
+    return CS_ERR_ARG;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+// arena.h -- device arena shared by all kernels: every cloth of a context is
+// packed into one set of arrays with global vertex / triangle / stencil /
+// block / node indices (a block-diagonal system of independent cloths).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "geom.cuh"
+
+namespace cs {
+
+// same layout as cs_params (include/clothgpu.h)
+struct DevParams {
+  double dt, lambda, myu, stiff_bend;
+  double gravity[3];
+  double mass_point, stiff_contact, contact_clearance;
+  double obs_center[3];
+  double obs_radius, tol;
+  int obstacle_kind, solver_kind, maxit, reserved;
+};
+
+// contact element as produced by the narrow phase
+struct Cand {
+  int k[4];     // canonical key (global vertex ids)
+  int fv;       // 1 face-vertex, 0 edge-edge
+  int na, nb;   // leaf nodes of the pair, na on the child-0 side of their common ancestor
+  int test;     // index of the elementary test within the pair (0..14)
+};
+
+// per-cloth control block kept on the device
+struct InstState {
+  int nlev;          // impulse levels of the current contact list
+  int n_contacts;    // contacts of the last detection
+  int impulse_applied;
+  int riz_nodes;
+  int solver_iterations;
+  int ilu_singular;
+  int done;          // solver converged
+  int pad;
+  double solver_conv;
+  double sq[2];      // CG: r.r of the previous / current iteration (by parity)
+  double inv0;
+  double rpr;        // PCG: r.Pr
+};
+
+struct Arena {
+  int ni = 0, nv = 0, nt = 0, nq = 0, nb = 0, nn = 0, ne = 0, nchunk = 0;
+  // per cloth
+  int* active = nullptr;  // takes part in the current pass
+  int *voff = nullptr, *toff = nullptr, *qoff = nullptr, *boff = nullptr, *noff = nullptr;
+  int *chunk_lo = nullptr, *chunk_hi = nullptr;  // row chunks of each cloth for the CG reductions
+  DevParams* prm = nullptr;
+  InstState* st = nullptr;
+  // vertices
+  double *x = nullptr, *v = nullptr, *x1 = nullptr, *X0 = nullptr, *v0 = nullptr;
+  int *bc = nullptr, *vinst = nullptr;
+  // elements
+  int *tri = nullptr, *tinst = nullptr, *quad = nullptr, *qinst = nullptr;
+  double *qK = nullptr, *qscale = nullptr;
+  double *tri_blk = nullptr, *tri_grad = nullptr, *quad_grad = nullptr;
+  // matrix (3x3 blocks, row-major), global rows
+  int *row_ptr = nullptr, *col_idx = nullptr, *dia_split = nullptr, *blk_row = nullptr;
+  int *slot_ptr = nullptr, *slot_src = nullptr, *grad_ptr = nullptr, *grad_src = nullptr;
+  double *vdia = nullptr, *vcrs = nullptr, *fdia = nullptr, *fcrs = nullptr;
+  // solver vectors (3 per vertex)
+  double *b = nullptr, *r = nullptr, *p = nullptr, *z = nullptr, *dx = nullptr;
+  double *part = nullptr;  // per-chunk partial sums
+  int* chunk_inst = nullptr;
+  // ILU(0) schedule: per cloth offsets into level tables
+  int *lev_off = nullptr, *lev_ptr = nullptr, *lev_rows = nullptr;
+  int *blev_off = nullptr, *blev_ptr = nullptr, *blev_rows = nullptr;
+  int *fac_ptr = nullptr, *fac_ops = nullptr, *sing = nullptr;
+  // BVH (global node ids; a leaf's child0 is a global triangle id)
+  int *node = nullptr, *pre = nullptr, *skip = nullptr, *leaf_lo = nullptr, *leaf_hi = nullptr;
+  int *depth = nullptr, *prepos = nullptr, *tri_leaf = nullptr, *refit_cnt = nullptr, *preoff = nullptr;
+  Box* box = nullptr;
+  // impact zones
+  int *edge_uv = nullptr, *uf = nullptr, *inzone = nullptr;
+};
+
+// scratch for the contact pipeline (grown on demand)
+struct ContactBufs {
+  int pair_cap = 0, cand_cap = 0, ce_cap = 0;
+  int2* pairs = nullptr;
+  Cand* cand = nullptr;
+  Cand* cand_sorted = nullptr;
+  unsigned long long *key_a = nullptr, *key_b = nullptr;
+  int *idx_a = nullptr, *idx_b = nullptr;
+  int* ce = nullptr;          // 5 ints per contact, sorted, deduplicated
+  int* ce_inst_lo = nullptr;  // per cloth segment of ce
+  int* ce_inst_hi = nullptr;
+  int* counters = nullptr;    // [0] pairs, [1] candidates, [2] contacts, [3] overflow flag
+  int* level = nullptr;       // impulse level per contact
+  int* order = nullptr;       // contacts grouped by level
+  int* lev_cnt = nullptr;     // per cloth: level count (then offsets)
+  int* vmark = nullptr;       // per vertex: last level touching it (stamped)
+  int* vstamp = nullptr;
+  int* zone_list = nullptr;   // in-zone vertices
+  unsigned long long* zkey = nullptr;
+  unsigned long long* zkey2 = nullptr;
+  double* zrec = nullptr;     // per vertex: zone record at its root (gc, av, omega)
+  void* cub_tmp = nullptr;
+  size_t cub_bytes = 0;
+};
+
+}  // namespace cs

@@ -1,0 +1,777 @@
+// k_collide.cu -- self-collision on the device (bvh_aabb.cpp,
+// self_collision_cloth.cpp), all FP64 with the reference's rounding.
+//
+// * refit: one thread per leaf; parents are merged by the second child to
+//   arrive (atomic counter per node), bottom-up in one launch.
+// * broad phase: one thread per triangle walks its cloth's BVH without a stack
+//   (depth-first preorder with skip links) and keeps the leaves to its right in
+//   leaf order, which is exactly the set and orientation of leaf pairs the
+//   reference's recursive descent visits.  Pairs are appended with
+//   warp-aggregated atomics.
+// * narrow phase: one thread per leaf pair runs the reference's 15 elementary
+//   tests and appends canonical contact elements.
+// * contact set: two stable radix sorts give the std::set order; a key seen
+//   more than once keeps the element the reference inserts first (decided by
+//   the reference's traversal order when face-vertex and edge-edge collide).
+// * impulses: contacts of a cloth are split into levels so that no two
+//   contacts of a level share a vertex and every contact follows all earlier
+//   contacts it shares a vertex with; levels run in order, which reproduces
+//   the reference's sequential Gauss-Seidel sweep exactly.
+// * impact zones: union-find over contact vertices and mesh edges, then one
+//   thread per zone sums its members in ascending order.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "kernels.h"
+
+namespace cs {
+namespace {
+
+constexpr int kT = 128;
+inline int nblk(long long n, int t = kT) { return (int)((n + t - 1) / t); }
+
+__device__ __forceinline__ Box load_box(const Box* b, int n) {
+  // boxes written by other threads in this launch: read around L1
+  Box r;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r.lo[k] = __ldcg(&b[n].lo[k]);
+    r.hi[k] = __ldcg(&b[n].hi[k]);
+  }
+  r.full = __ldcg(&b[n].full);
+  return r;
+}
+
+__device__ __forceinline__ V3<double> end_pos(const double* x, const double* v, int i, double dt) {
+  return mk<double>(x[3 * i + 0] + dt * v[3 * i + 0], x[3 * i + 1] + dt * v[3 * i + 1], x[3 * i + 2] + dt * v[3 * i + 2]);
+}
+
+// BuildBoundingBoxChild_Prx / _CCD (bvh_aabb.cpp:23-106)
+__global__ void k_refit(Arena A, int ccd, const double* xs, const double* vs, double delta_override) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nt) return;
+  const int inst = A.tinst[t];
+  if (!A.active[inst]) return;
+  const DevParams& P = A.prm[inst];
+  Box b;
+  box_clear(b);
+  const double delta = delta_override >= 0 ? delta_override : P.contact_clearance;
+  const double eps = ccd ? 1.0e-10 : delta * 0.5;
+  int vid[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    vid[a] = A.tri[3 * t + a];
+    box_add(b, ld3(xs, vid[a]), eps);
+  }
+  if (ccd) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) box_add(b, end_pos(xs, vs, vid[a], P.dt), eps);
+  }
+  int n = A.tri_leaf[t];
+  A.box[n] = b;
+  for (;;) {
+    __threadfence();
+    const int par = A.node[3 * n + 0];
+    if (par < 0) break;
+    if (atomicAdd(&A.refit_cnt[par], 1) == 0) break;  // the sibling finishes the parent
+    Box m = load_box(A.box, A.node[3 * par + 1]);
+    box_merge(m, load_box(A.box, A.node[3 * par + 2]));
+    A.box[par] = m;
+    n = par;
+  }
+}
+
+__device__ __forceinline__ int warp_append(int* counter) {
+  const unsigned m = __activemask();
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(m, base, leader);
+  return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// broad phase: leaf pairs with overlapping boxes (GetContactElement_* recursion,
+// bvh_aabb.cpp:441-557 / 797-923)
+__global__ void k_traverse(Arena A, ContactBufs C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nt) return;
+  const int inst = A.tinst[t];
+  if (!A.active[inst]) return;
+  const int la = A.tri_leaf[t];
+  const int oa = A.leaf_lo[la];
+  const Box ba = A.box[la];
+  int k = A.preoff[inst];
+  const int end = A.preoff[inst + 1];
+  while (k < end) {
+    const int n = A.pre[k];
+    if (A.leaf_hi[n] <= oa || !box_overlap(ba, A.box[n])) {
+      k = A.skip[k];
+      continue;
+    }
+    if (A.node[3 * n + 2] == -1) {
+      const int slot = warp_append(&C.counters[0]);
+      if (slot < C.pair_cap)
+        C.pairs[slot] = make_int2(la, n);
+      else
+        C.counters[3] = 1;
+      k = A.skip[k];
+    } else {
+      k++;
+    }
+  }
+}
+
+// canonical key (CContactElement constructor, bvh_aabb.h:68-93)
+__device__ __forceinline__ void canonical(int fv, int j0, int j1, int j2, int j3, int k[4]) {
+  if (fv) {
+    int a = j0, b = j1, c = j2, t;
+    if (a > b) { t = a; a = b; b = t; }
+    if (b > c) { t = b; b = c; c = t; }
+    if (a > b) { t = a; a = b; b = t; }
+    k[0] = a; k[1] = b; k[2] = c; k[3] = j3;
+  } else {
+    const int lo01 = j0 < j1 ? j0 : j1, lo23 = j2 < j3 ? j2 : j3;
+    int o0, o1;
+    if (lo01 < lo23) {
+      k[0] = lo01; k[1] = (j0 < j1) ? j1 : j0; o0 = j2; o1 = j3;
+    } else {
+      k[0] = lo23; k[1] = (j2 < j3) ? j3 : j2; o0 = j0; o1 = j1;
+    }
+    k[2] = o0 < o1 ? o0 : o1;
+    k[3] = o0 < o1 ? o1 : o0;
+  }
+}
+
+__device__ __forceinline__ void emit(const ContactBufs& C, int fv, int j0, int j1, int j2, int j3, int na, int nb,
+                                     int test) {
+  const int slot = warp_append(&C.counters[1]);
+  if (slot >= C.cand_cap) {
+    C.counters[3] = 1;
+    return;
+  }
+  Cand c;
+  canonical(fv, j0, j1, j2, j3, c.k);
+  c.fv = fv;
+  c.na = na;
+  c.nb = nb;
+  c.test = test;
+  C.cand[slot] = c;
+}
+
+// the 9 edge pairs of a triangle pair, in the reference's order
+__constant__ int kEE[9][4] = {{0, 1, 0, 1}, {0, 1, 1, 2}, {0, 1, 2, 0}, {1, 2, 0, 1}, {1, 2, 1, 2},
+                              {1, 2, 2, 0}, {2, 0, 0, 1}, {2, 0, 1, 2}, {2, 0, 2, 0}};
+
+// narrow phase of one leaf pair (bvh_aabb.cpp:473-536 proximity, 836-901 CCD)
+__global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs, double delta_override,
+                         int npairs) {
+  const int pid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pid >= npairs) return;
+  const int2 pr = C.pairs[pid];
+  const int na = pr.x, nb = pr.y;
+  const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
+  const int inst = A.tinst[ta];
+  const DevParams& P = A.prm[inst];
+  const double delta = delta_override >= 0 ? delta_override : P.contact_clearance;
+  int ia[3], ib[3];
+  V3<double> p[3], q[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    ia[k] = A.tri[3 * ta + k];
+    ib[k] = A.tri[3 * tb + k];
+    p[k] = ld3(xs, ia[k]);
+    q[k] = ld3(xs, ib[k]);
+  }
+  if (!ccd) {
+    // the reference passes aBB[triangle index]: the box of the node whose
+    // index equals the triangle's index within its cloth
+    const Box bba = A.box[A.noff[inst] + (ta - A.toff[inst])];
+    const Box bbb = A.box[A.noff[inst] + (tb - A.toff[inst])];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      if (fv_proximity(ia[0], ia[1], ia[2], ib[k], p[0], p[1], p[2], q[k], bba, delta))
+        emit(C, 1, ia[0], ia[1], ia[2], ib[k], na, nb, k);
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      if (fv_proximity(ib[0], ib[1], ib[2], ia[k], q[0], q[1], q[2], p[k], bbb, delta))
+        emit(C, 1, ib[0], ib[1], ib[2], ia[k], na, nb, 3 + k);
+    for (int k = 0; k < 9; k++) {
+      const int e0 = kEE[k][0], e1 = kEE[k][1], f0 = kEE[k][2], f1 = kEE[k][3];
+      if (ee_proximity(ia[e0], ia[e1], ib[f0], ib[f1], p[e0], p[e1], q[f0], q[f1], delta))
+        emit(C, 0, ia[e0], ia[e1], ib[f0], ib[f1], na, nb, 6 + k);
+    }
+  } else {
+    V3<double> pe[3], qe[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      pe[k] = end_pos(xs, vs, ia[k], P.dt);
+      qe[k] = end_pos(xs, vs, ib[k], P.dt);
+    }
+    const Box bba = A.box[na], bbb = A.box[nb];
+    for (int k = 0; k < 3; k++)
+      if (fv_ccd(ia[0], ia[1], ia[2], ib[k], p[0], p[1], p[2], q[k], pe[0], pe[1], pe[2], qe[k], bba))
+        emit(C, 1, ia[0], ia[1], ia[2], ib[k], na, nb, k);
+    for (int k = 0; k < 3; k++)
+      if (fv_ccd(ib[0], ib[1], ib[2], ia[k], q[0], q[1], q[2], p[k], qe[0], qe[1], qe[2], pe[k], bbb))
+        emit(C, 1, ib[0], ib[1], ib[2], ia[k], na, nb, 3 + k);
+    for (int k = 0; k < 9; k++) {
+      const int e0 = kEE[k][0], e1 = kEE[k][1], f0 = kEE[k][2], f1 = kEE[k][3];
+      if (ee_ccd(ia[e0], ia[e1], ib[f0], ib[f1], p[e0], p[e1], q[f0], q[f1], pe[e0], pe[e1], qe[f0], qe[f1]))
+        emit(C, 0, ia[e0], ia[e1], ib[f0], ib[f1], na, nb, 6 + k);
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long key_hi(const Cand& c) {
+  return ((unsigned long long)(unsigned)c.k[0] << 32) | (unsigned)c.k[1];
+}
+__device__ __forceinline__ unsigned long long key_lo(const Cand& c) {
+  return ((unsigned long long)(unsigned)c.k[2] << 32) | (unsigned)c.k[3];
+}
+
+__global__ void k_keys_lo(ContactBufs C, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  C.key_a[i] = key_lo(C.cand[i]);
+  C.idx_a[i] = i;
+}
+
+__global__ void k_keys_hi(ContactBufs C, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  C.key_a[i] = key_hi(C.cand[C.idx_b[i]]);
+}
+
+__global__ void k_gather_cand(ContactBufs C, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  C.cand_sorted[i] = C.cand[C.idx_a[i]];
+}
+
+__device__ __forceinline__ bool same_key(const Cand& a, const Cand& b) {
+  return a.k[0] == b.k[0] && a.k[1] == b.k[1] && a.k[2] == b.k[2] && a.k[3] == b.k[3];
+}
+
+constexpr int kMaxDepth = 128;
+
+// child choices (0 / 1) from below `top` down to `leaf`, top-down; returns the count
+__device__ int path_bits(const Arena& A, int top, int leaf, unsigned char* bits) {
+  int n = 0;
+  int cur = leaf;
+  while (cur != top && n < kMaxDepth) {
+    const int par = A.node[3 * cur];
+    bits[n++] = (A.node[3 * par + 2] == cur) ? 1 : 0;
+    cur = par;
+  }
+  for (int i = 0; i < n / 2; i++) {
+    const unsigned char t = bits[i];
+    bits[i] = bits[n - 1 - i];
+    bits[n - 1 - i] = t;
+  }
+  return n;
+}
+
+__device__ int lca(const Arena& A, int a, int b) {
+  while (A.depth[a] > A.depth[b]) a = A.node[3 * a];
+  while (A.depth[b] > A.depth[a]) b = A.node[3 * b];
+  while (a != b) {
+    a = A.node[3 * a];
+    b = A.node[3 * b];
+  }
+  return a;
+}
+
+// True when the reference's recursive traversal reaches candidate x before y.
+// Pairs are visited grouped by their lowest common ancestor in depth-first
+// preorder (walk_self: pair(child0, child1), then each subtree); within one
+// ancestor the simultaneous descent of walk_pair orders children as
+// (0,0), (1,0), (0,1), (1,1) while both sides are internal, then by the side
+// still internal; within a leaf pair, by test index.
+__device__ bool visited_before(const Arena& A, const Cand& x, const Cand& y) {
+  const int lx = lca(A, x.na, x.nb), ly = lca(A, y.na, y.nb);
+  if (lx != ly) return A.prepos[lx] < A.prepos[ly];
+  if (x.na == y.na && x.nb == y.nb) return x.test < y.test;
+  const int c0 = A.node[3 * lx + 1], c1 = A.node[3 * lx + 2];
+  unsigned char xa[kMaxDepth], xb[kMaxDepth], ya[kMaxDepth], yb[kMaxDepth];
+  const int mxa = path_bits(A, c0, x.na, xa), mxb = path_bits(A, c1, x.nb, xb);
+  const int mya = path_bits(A, c0, y.na, ya), myb = path_bits(A, c1, y.nb, yb);
+  for (int k = 0;; k++) {
+    const bool xi = k < mxa || k < mxb, yi = k < mya || k < myb;
+    if (!xi || !yi) return xi < yi;  // unreachable for distinct pairs
+    const int dx = (k < mxa && k < mxb) ? xa[k] + 2 * xb[k] : (k < mxa ? xa[k] : xb[k]);
+    const int dy = (k < mya && k < myb) ? ya[k] + 2 * yb[k] : (k < mya ? ya[k] : yb[k]);
+    if (dx != dy) return dx < dy;
+  }
+}
+
+// run heads of the sorted candidates and the element std::set keeps for each key
+__global__ void k_dedupe(Arena A, ContactBufs C, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Cand ci = C.cand_sorted[i];
+  const bool head = (i == 0) || !same_key(C.cand_sorted[i - 1], ci);
+  C.idx_b[i] = head ? 1 : 0;
+  if (!head) return;
+  int j = i + 1;
+  bool mixed = false;
+  while (j < n && same_key(C.cand_sorted[j], ci)) {
+    mixed |= (C.cand_sorted[j].fv != ci.fv);
+    j++;
+  }
+  int win = i;
+  if (mixed)
+    for (int k = i + 1; k < j; k++)
+      if (visited_before(A, C.cand_sorted[k], C.cand_sorted[win])) win = k;
+  C.level[i] = C.cand_sorted[win].fv;
+}
+
+__global__ void k_compact(Arena A, ContactBufs C, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int pos = C.idx_a[i];
+  if (i == n - 1) C.counters[2] = pos + C.idx_b[i];
+  if (!C.idx_b[i]) return;
+  const Cand c = C.cand_sorted[i];
+  C.ce[5 * pos + 0] = C.level[i];
+  C.ce[5 * pos + 1] = c.k[0];
+  C.ce[5 * pos + 2] = c.k[1];
+  C.ce[5 * pos + 3] = c.k[2];
+  C.ce[5 * pos + 4] = c.k[3];
+}
+
+// per-cloth segments of the contact list (contacts of one cloth are contiguous
+// because vertex ids of a cloth are contiguous and lists are sorted)
+__global__ void k_segments(Arena A, ContactBufs C) {
+  const int n = C.counters[2];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int inst = A.vinst[C.ce[5 * e + 1]];
+  if (e == 0 || A.vinst[C.ce[5 * (e - 1) + 1]] != inst) C.ce_inst_lo[inst] = e;
+  if (e == n - 1 || A.vinst[C.ce[5 * (e + 1) + 1]] != inst) C.ce_inst_hi[inst] = e + 1;
+}
+
+__global__ void k_counts(Arena A, ContactBufs C) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= A.ni) return;
+  A.st[inst].n_contacts = A.active[inst] ? C.ce_inst_hi[inst] - C.ce_inst_lo[inst] : 0;
+  A.st[inst].riz_nodes = 0;
+}
+
+// ---- impulses (self_collision_cloth.cpp:20-212) ------------------------------
+// levels of the sequential sweep, one thread per cloth
+__global__ void k_impulse_levels(Arena A, ContactBufs C, int token) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= A.ni) return;
+  A.st[inst].nlev = 0;
+  if (!A.active[inst]) return;
+  const int lo = C.ce_inst_lo[inst], hi = C.ce_inst_hi[inst];
+  if (lo >= hi) return;
+  int nlev = 0;
+  for (int c = lo; c < hi; c++) {
+    int l = 0;
+#pragma unroll
+    for (int k = 1; k <= 4; k++) {
+      const int v = C.ce[5 * c + k];
+      if (C.vstamp[v] == token) l = max(l, C.vmark[v] + 1);
+    }
+#pragma unroll
+    for (int k = 1; k <= 4; k++) {
+      const int v = C.ce[5 * c + k];
+      C.vmark[v] = l;
+      C.vstamp[v] = token;
+    }
+    C.level[c] = l;
+    nlev = max(nlev, l + 1);
+  }
+  int* off = C.lev_cnt + lo + inst;  // nlev + 1 counters, disjoint per cloth
+  for (int l = 0; l <= nlev; l++) off[l] = 0;
+  for (int c = lo; c < hi; c++) off[C.level[c] + 1]++;
+  for (int l = 0; l < nlev; l++) off[l + 1] += off[l];
+  for (int c = lo; c < hi; c++) C.order[lo + off[C.level[c]]++] = c;
+  for (int l = nlev; l > 0; l--) off[l] = off[l - 1];
+  off[0] = 0;
+  A.st[inst].nlev = nlev;
+}
+
+__device__ __forceinline__ void add_v(double* v, int i, double a, double b, double c) {
+  v[3 * i + 0] += a;
+  v[3 * i + 1] += b;
+  v[3 * i + 2] += c;
+}
+
+// one contact of the sweep (SelfCollisionImpulse_Proximity / _CCD)
+__device__ void impulse_one(const DevParams& P, const int* e, const double* x, double* v, int ccd) {
+  const double delta = P.contact_clearance, stiff = P.stiff_contact, dt = P.dt, mass = P.mass_point;
+  const int i0 = e[1], i1 = e[2], i2 = e[3], i3 = e[4];
+  const V3<double> p0 = ld3(x, i0), p1 = ld3(x, i1), p2 = ld3(x, i2), p3 = ld3(x, i3);
+  const V3<double> v0 = ld3((const double*)v, i0), v1 = ld3((const double*)v, i1), v2 = ld3((const double*)v, i2),
+                   v3 = ld3((const double*)v, i3);
+  double t = 0;
+  if (ccd) {
+    t = coplanar_time(p0, p1, p2, p3, p0 + v0, p1 + v1, p2 + v2, p3 + v3);
+    if (t < 0 || t > 1) return;
+  }
+  if (e[0]) {  // face (i0 i1 i2) - vertex i3
+    double w0, w1;
+    const double dist = ccd ? dist_face_vertex(p0 + t * v0, p1 + t * v1, p2 + t * v2, p3 + t * v3, w0, w1)
+                            : dist_face_vertex(p0, p1, p2, p3, w0, w1);
+    if (w0 < 0 || w0 > 1) return;
+    if (w1 < 0 || w1 > 1) return;
+    if (dist > delta) return;
+    const double w2 = 1.0 - w0 - w1;
+    const V3<double> pc = w0 * p0 + w1 * p1 + w2 * p2;
+    const V3<double> nrm = normalized(p3 - pc);
+    const double rel_v = dot(v3 - w0 * v0 - w1 * v1 - w2 * v2, nrm);
+    double imp_mod;
+    if (!ccd) {
+      const double depth = delta - dot(p3 - pc, nrm);
+      if (rel_v > 0.1 * depth / dt) return;
+      const double imp_el = dt * stiff * depth;
+      const double imp_ie = mass * (0.1 * depth / dt - rel_v);
+      const double imp_min = (imp_el < imp_ie) ? imp_el : imp_ie;
+      imp_mod = 2 * imp_min / (1 + w0 * w0 + w1 * w1 + w2 * w2);
+      imp_mod /= mass;
+      imp_mod *= 0.25;
+    } else {
+      if (rel_v > 0.1 * delta / dt) return;
+      const double imp = mass * (0.1 * delta / dt - rel_v);
+      imp_mod = 2 * imp / (1.0 + w0 * w0 + w1 * w1 + w2 * w2);
+      imp_mod /= mass;
+      imp_mod *= 0.1;
+    }
+    const double mx = -nrm.x, my = -nrm.y, mz = -nrm.z;
+    add_v(v, i0, mx * imp_mod * w0, my * imp_mod * w0, mz * imp_mod * w0);
+    add_v(v, i1, mx * imp_mod * w1, my * imp_mod * w1, mz * imp_mod * w1);
+    add_v(v, i2, mx * imp_mod * w2, my * imp_mod * w2, mz * imp_mod * w2);
+    add_v(v, i3, nrm.x * imp_mod, nrm.y * imp_mod, nrm.z * imp_mod);
+  } else {  // edge (i0 i1) - edge (i2 i3)
+    double w01, w23;
+    const double dist = ccd ? dist_edge_edge(p0 + t * v0, p1 + t * v1, p2 + t * v2, p3 + t * v3, w01, w23)
+                            : dist_edge_edge(p0, p1, p2, p3, w01, w23);
+    if (w01 < 0 || w01 > 1) return;
+    if (w23 < 0 || w23 > 1) return;
+    if (dist > delta) return;
+    const V3<double> c01 = (1 - w01) * p0 + w01 * p1;
+    const V3<double> c23 = (1 - w23) * p2 + w23 * p3;
+    const V3<double> nrm = normalized(c23 - c01);
+    const double rel_v = dot((1 - w23) * v2 + w23 * v3 - (1 - w01) * v0 - w01 * v1, nrm);
+    const double wsum = w01 * w01 + (1 - w01) * (1 - w01) + w23 * w23 + (1 - w23) * (1 - w23);
+    double imp_mod;
+    if (!ccd) {
+      const double depth = delta - length(c23 - c01);
+      if (rel_v > 0.1 * depth / dt) return;
+      const double imp_el = dt * stiff * depth;
+      const double imp_ie = mass * (0.1 * depth / dt - rel_v);
+      const double imp_min = (imp_el < imp_ie) ? imp_el : imp_ie;
+      imp_mod = 2 * imp_min / wsum;
+      imp_mod /= mass;
+      imp_mod *= 0.25;
+    } else {
+      if (rel_v > 0.1 * delta / dt) return;
+      const double imp = mass * (0.1 * delta / dt - rel_v);
+      imp_mod = 2 * imp / wsum;
+      imp_mod /= mass;
+      imp_mod *= 0.1;
+    }
+    const double mx = -nrm.x, my = -nrm.y, mz = -nrm.z;
+    add_v(v, i0, mx * imp_mod * (1 - w01), my * imp_mod * (1 - w01), mz * imp_mod * (1 - w01));
+    add_v(v, i1, mx * imp_mod * w01, my * imp_mod * w01, mz * imp_mod * w01);
+    add_v(v, i2, nrm.x * imp_mod * (1 - w23), nrm.y * imp_mod * (1 - w23), nrm.z * imp_mod * (1 - w23));
+    add_v(v, i3, nrm.x * imp_mod * w23, nrm.y * imp_mod * w23, nrm.z * imp_mod * w23);
+  }
+}
+
+// one CTA per cloth applies its levels in order
+__global__ void k_impulse_apply(Arena A, ContactBufs C, int ccd, const double* xs, double* vs) {
+  const int inst = blockIdx.x;
+  if (!A.active[inst]) return;
+  const int nlev = A.st[inst].nlev;
+  if (nlev == 0) return;
+  const int lo = C.ce_inst_lo[inst];
+  const int* off = C.lev_cnt + lo + inst;
+  const DevParams& P = A.prm[inst];
+  for (int l = 0; l < nlev; l++) {
+    for (int j = off[l] + threadIdx.x; j < off[l + 1]; j += blockDim.x)
+      impulse_one(P, C.ce + 5 * C.order[lo + j], xs, vs, ccd);
+    __syncthreads();
+  }
+}
+
+// ---- rigid impact zones (self_collision_cloth.cpp:220-348) --------------------
+__device__ int uf_find(int* uf, int x) {
+  volatile int* u = uf;
+  int p = u[x];
+  while (p != x) {
+    x = p;
+    p = u[x];
+  }
+  return x;
+}
+
+// link the larger root under the smaller; parents only decrease, so every
+// find terminates, and each failed exchange means another thread made progress
+__device__ void uf_union(int* uf, int a, int b) {
+  for (;;) {
+    a = uf_find(uf, a);
+    b = uf_find(uf, b);
+    if (a == b) return;
+    if (a > b) {
+      const int t = a;
+      a = b;
+      b = t;
+    }
+    if (atomicCAS(&uf[b], b, a) == b) return;
+  }
+}
+
+__global__ void k_riz_reset(Arena A) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv || !A.active[A.vinst[v]]) return;
+  A.uf[v] = v;
+  A.inzone[v] = 0;
+}
+
+__global__ void k_riz_count(Arena A) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  const int inst = A.vinst[v];
+  if (A.active[inst] && A.inzone[v]) atomicAdd(&A.st[inst].riz_nodes, 1);
+}
+
+__global__ void k_riz_contacts(Arena A, ContactBufs C, int nce) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nce) return;
+  const int* e = C.ce + 5 * c;
+  if (!A.active[A.vinst[e[1]]]) return;
+#pragma unroll
+  for (int k = 1; k <= 4; k++) A.inzone[e[k]] = 1;
+  uf_union(A.uf, e[1], e[2]);
+  uf_union(A.uf, e[1], e[3]);
+  uf_union(A.uf, e[1], e[4]);
+}
+
+// a contact joins every zone holding one of its vertices or a 1-ring
+// neighbour of one: mesh edges between zone vertices merge their zones
+__global__ void k_riz_edges(Arena A) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= A.ne) return;
+  const int u = A.edge_uv[2 * e], w = A.edge_uv[2 * e + 1];
+  if (!A.active[A.vinst[u]]) return;
+  if (A.inzone[u] && A.inzone[w]) uf_union(A.uf, u, w);
+}
+
+__global__ void k_riz_collect(Arena A, ContactBufs C, int* count) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  if (!A.active[A.vinst[v]] || !A.inzone[v]) return;
+  const int root = uf_find(A.uf, v);
+  const int pos = atomicAdd(count, 1);
+  C.zkey[pos] = ((unsigned long long)(unsigned)root << 32) | (unsigned)v;
+}
+
+// per zone: centroid, mean velocity, angular momentum and the reference's
+// "inertia" (diagonal |v|^2 - q_i^2), all summed over members in ascending order
+__global__ void k_riz_stats(Arena A, ContactBufs C, int n, const double* xs, const double* v0s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long* z = C.zkey2;
+  const unsigned root = (unsigned)(z[i] >> 32);
+  if (i > 0 && (unsigned)(z[i - 1] >> 32) == root) return;
+  int j = i;
+  V3<double> gc = mk(0.0, 0.0, 0.0), av = mk(0.0, 0.0, 0.0);
+  while (j < n && (unsigned)(z[j] >> 32) == root) {
+    const int m = (int)(unsigned)(z[j] & 0xffffffffull);
+    gc = gc + ld3(xs, m);
+    av = av + ld3(v0s, m);
+    j++;
+  }
+  const double cnt = (double)(j - i);
+  gc = div_guarded(gc, cnt);
+  av = div_guarded(av, cnt);
+  V3<double> L = mk(0.0, 0.0, 0.0);
+  double I[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = i; k < j; k++) {
+    const int m = (int)(unsigned)(z[k] & 0xffffffffull);
+    const V3<double> p = ld3(xs, m), u = ld3(v0s, m);
+    const V3<double> q = p - gc;
+    const double uu = dot(u, u);
+    L = L + cross(p - gc, u - av);
+    I[0] += uu - q.x * q.x;
+    I[1] += -q.x * q.y;
+    I[2] += -q.x * q.z;
+    I[3] += -q.y * q.x;
+    I[4] += uu - q.y * q.y;
+    I[5] += -q.y * q.z;
+    I[6] += -q.z * q.x;
+    I[7] += -q.z * q.y;
+    I[8] += uu - q.z * q.z;
+  }
+  // CalcInvMat3 of self_collision_cloth.cpp:278-296
+  const double det = +I[0] * I[4] * I[8] + I[3] * I[7] * I[2] + I[6] * I[1] * I[5] - I[0] * I[7] * I[5] -
+                     I[6] * I[4] * I[2] - I[3] * I[1] * I[8];
+  const double r = 1.0 / det;
+  double Iv[9];
+  Iv[0] = r * (I[4] * I[8] - I[5] * I[7]);
+  Iv[1] = r * (I[2] * I[7] - I[1] * I[8]);
+  Iv[2] = r * (I[1] * I[5] - I[2] * I[4]);
+  Iv[3] = r * (I[5] * I[6] - I[3] * I[8]);
+  Iv[4] = r * (I[0] * I[8] - I[2] * I[6]);
+  Iv[5] = r * (I[2] * I[3] - I[0] * I[5]);
+  Iv[6] = r * (I[3] * I[7] - I[4] * I[6]);
+  Iv[7] = r * (I[1] * I[6] - I[0] * I[7]);
+  Iv[8] = r * (I[0] * I[4] - I[1] * I[3]);
+  double* rec = C.zrec + 9 * (size_t)root;
+  rec[0] = gc.x;
+  rec[1] = gc.y;
+  rec[2] = gc.z;
+  rec[3] = av.x;
+  rec[4] = av.y;
+  rec[5] = av.z;
+  rec[6] = Iv[0] * L.x + Iv[1] * L.y + Iv[2] * L.z;
+  rec[7] = Iv[3] * L.x + Iv[4] * L.y + Iv[5] * L.z;
+  rec[8] = Iv[6] * L.x + Iv[7] * L.y + Iv[8] * L.z;
+}
+
+__global__ void k_riz_velocity(ContactBufs C, int n, const double* xs, double* vs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned root = (unsigned)(C.zkey2[i] >> 32);
+  const int m = (int)(unsigned)(C.zkey2[i] & 0xffffffffull);
+  const double* rec = C.zrec + 9 * (size_t)root;
+  const V3<double> gc = mk(rec[0], rec[1], rec[2]), omg = mk(rec[6], rec[7], rec[8]);
+  const V3<double> rot = cross(ld3(xs, m) - gc, omg);
+  vs[3 * m + 0] = rec[3] + (-rot.x);
+  vs[3 * m + 1] = rec[4] + (-rot.y);
+  vs[3 * m + 2] = rec[5] + (-rot.z);
+}
+
+__global__ void k_riz_labels(Arena A, int* zone_of) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  zone_of[v] = (A.active[A.vinst[v]] && A.inzone[v]) ? uf_find(A.uf, v) : -1;
+}
+
+}  // namespace
+
+// ---- launchers ----------------------------------------------------------------
+void launch_refit(const Arena& A, int ccd, const double* xs, const double* vs, double delta_override,
+                  cudaStream_t s) {
+  cudaMemsetAsync(A.refit_cnt, 0, sizeof(int) * (size_t)A.nn, s);
+  k_refit<<<nblk(A.nt), kT, 0, s>>>(A, ccd, xs, vs, delta_override);
+  g_launches++;
+}
+
+void launch_traverse(const Arena& A, const ContactBufs& C, cudaStream_t s) {
+  k_traverse<<<nblk(A.nt), kT, 0, s>>>(A, C);
+  g_launches++;
+}
+
+void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
+                   double delta_override, int npairs, cudaStream_t s) {
+  if (npairs <= 0) return;
+  k_narrow<<<nblk(npairs), kT, 0, s>>>(A, C, ccd, xs, vs, delta_override, npairs);
+  g_launches++;
+}
+
+size_t cub_sort_bytes(int n) {
+  size_t b1 = 0, b2 = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, b1, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                  (int*)nullptr, (int*)nullptr, n);
+  cub::DeviceScan::ExclusiveSum(nullptr, b2, (int*)nullptr, (int*)nullptr, n);
+  return b1 > b2 ? b1 : b2;
+}
+
+void cub_sort_pairs(void* tmp, size_t bytes, const unsigned long long* kin, unsigned long long* kout, const int* vin,
+                    int* vout, int n, cudaStream_t s) {
+  cub::DeviceRadixSort::SortPairs(tmp, bytes, kin, kout, vin, vout, n, 0, 64, s);
+  g_launches += 4;
+}
+
+void cub_sort_keys(void* tmp, size_t bytes, const unsigned long long* kin, unsigned long long* kout, int n,
+                   cudaStream_t s) {
+  cub::DeviceRadixSort::SortKeys(tmp, bytes, kin, kout, n, 0, 64, s);
+  g_launches += 4;
+}
+
+void cub_exclusive_sum(void* tmp, size_t bytes, const int* in, int* out, int n, cudaStream_t s) {
+  cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, n, s);
+  g_launches += 2;
+}
+
+void sort_dedupe(const Arena& A, ContactBufs& C, int n, cudaStream_t s) {
+  cudaMemsetAsync(C.ce_inst_lo, 0, sizeof(int) * (size_t)A.ni, s);
+  cudaMemsetAsync(C.ce_inst_hi, 0, sizeof(int) * (size_t)A.ni, s);
+  if (n <= 0) {
+    cudaMemsetAsync(C.counters + 2, 0, sizeof(int), s);
+    k_counts<<<nblk(A.ni), kT, 0, s>>>(A, C);
+    g_launches++;
+    return;
+  }
+  // lexicographic (k0, k1, k2, k3): stable sort by the low pair, then the high pair
+  k_keys_lo<<<nblk(n), kT, 0, s>>>(C, n);
+  cub_sort_pairs(C.cub_tmp, C.cub_bytes, C.key_a, C.key_b, C.idx_a, C.idx_b, n, s);
+  k_keys_hi<<<nblk(n), kT, 0, s>>>(C, n);
+  cub_sort_pairs(C.cub_tmp, C.cub_bytes, C.key_a, C.key_b, C.idx_b, C.idx_a, n, s);
+  k_gather_cand<<<nblk(n), kT, 0, s>>>(C, n);
+  k_dedupe<<<nblk(n), kT, 0, s>>>(A, C, n);
+  cub_exclusive_sum(C.cub_tmp, C.cub_bytes, C.idx_b, C.idx_a, n, s);
+  k_compact<<<nblk(n), kT, 0, s>>>(A, C, n);
+  k_segments<<<nblk(n), kT, 0, s>>>(A, C);
+  k_counts<<<nblk(A.ni), kT, 0, s>>>(A, C);
+  g_launches += 7;
+}
+
+void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, int token,
+                     cudaStream_t s) {
+  k_impulse_levels<<<nblk(A.ni, 32), 32, 0, s>>>(A, C, token);
+  k_impulse_apply<<<A.ni, 128, 0, s>>>(A, C, ccd, xs, vs);
+  g_launches += 2;
+}
+
+void launch_riz_reset(const Arena& A, cudaStream_t s) {
+  k_riz_reset<<<nblk(A.nv), kT, 0, s>>>(A);
+  g_launches++;
+}
+
+void launch_riz_add(const Arena& A, const ContactBufs& C, int nce, cudaStream_t s) {
+  if (nce > 0) {
+    k_riz_contacts<<<nblk(nce), kT, 0, s>>>(A, C, nce);
+    g_launches++;
+  }
+  if (A.ne > 0) {
+    k_riz_edges<<<nblk(A.ne), kT, 0, s>>>(A);
+    g_launches++;
+  }
+}
+
+// rigid velocities of all zones of the active cloths; returns nothing, uses
+// C.counters[4] as the member count
+void riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, const double* v0s, cudaStream_t s) {
+  int* cnt = C.counters + 4;
+  cudaMemsetAsync(cnt, 0, sizeof(int), s);
+  k_riz_collect<<<nblk(A.nv), kT, 0, s>>>(A, C, cnt);
+  g_launches++;
+  int n = 0;
+  cudaMemcpyAsync(&n, cnt, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  if (n == 0) return;
+  cub_sort_keys(C.cub_tmp, C.cub_bytes, C.zkey, C.zkey2, n, s);
+  k_riz_stats<<<nblk(n), kT, 0, s>>>(A, C, n, xs, v0s);
+  k_riz_velocity<<<nblk(n), kT, 0, s>>>(C, n, xs, vs);
+  g_launches += 2;
+}
+
+int riz_count_zones(const Arena& A, ContactBufs& C, int* zone_of, cudaStream_t s) {
+  k_riz_labels<<<nblk(A.nv), kT, 0, s>>>(A, zone_of);
+  g_launches++;
+  (void)C;
+  return 0;
+}
+
+void launch_riz_count(const Arena& A, cudaStream_t s) {
+  k_riz_count<<<nblk(A.nv), kT, 0, s>>>(A);
+  g_launches++;
+}
+
+}  // namespace cs

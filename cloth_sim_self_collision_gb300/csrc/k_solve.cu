@@ -1,0 +1,451 @@
+// k_solve.cu -- linear solvers of the implicit step.
+//
+// * Block ILU(0) + PCG (CPreconditionerILU / Solve_PCG, ilu_sparse.cpp:352-709):
+//   one CTA per cloth runs the factorisation and the whole PCG loop.  Rows are
+//   processed in dependency levels of the natural-order factorisation (and of
+//   the forward / backward sweeps), separated by __syncthreads, so every row
+//   is computed with exactly the reference's operation order; only the inner
+//   products are tree-summed (deterministically).
+// * CG (Solve_CG, matrix_square_sparse.cpp:338-406): three grid-wide kernels
+//   per iteration over the rows of all active cloths; per-cloth reductions go
+//   through per-chunk partials summed in a fixed order.
+#include <float.h>
+
+#include "kernels.h"
+
+namespace cs {
+namespace {
+
+constexpr int kSolveThreads = 512;
+constexpr int kChunk = 256;  // rows per CG chunk (one CTA)
+
+__device__ __forceinline__ double det33(const double* a) {
+  return +a[0] * a[4] * a[8] + a[3] * a[7] * a[2] + a[6] * a[1] * a[5] - a[0] * a[7] * a[5] -
+         a[6] * a[4] * a[2] - a[3] * a[1] * a[8];
+}
+
+// CalcInvMat3 (ilu_sparse.cpp:76-97): cofactor inverse into out from t
+__device__ __forceinline__ void inv33(double* out, const double* t) {
+  const double r = 1.0 / det33(t);
+  out[0] = r * (t[4] * t[8] - t[5] * t[7]);
+  out[1] = r * (t[2] * t[7] - t[1] * t[8]);
+  out[2] = r * (t[1] * t[5] - t[2] * t[4]);
+  out[3] = r * (t[5] * t[6] - t[3] * t[8]);
+  out[4] = r * (t[0] * t[8] - t[2] * t[6]);
+  out[5] = r * (t[2] * t[3] - t[0] * t[5]);
+  out[6] = r * (t[3] * t[7] - t[4] * t[6]);
+  out[7] = r * (t[1] * t[6] - t[0] * t[7]);
+  out[8] = r * (t[0] * t[4] - t[1] * t[3]);
+}
+
+// Deterministic block-wide sum: fixed xor-shuffle tree per warp, then the
+// warp totals in warp order.  All threads receive the result.
+__device__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) sh[32] = t;
+  }
+  __syncthreads();
+  return sh[32];
+}
+
+// <a, b> over dofs [lo, hi) of a cloth, by one CTA
+__device__ double cta_dot(const double* a, const double* b, int lo, int hi, double* sh) {
+  double s = 0.0;
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) s += a[i] * b[i];
+  return block_sum(s, sh);
+}
+
+// y_i = 0 * y_i + sum_j A_ij x_j for row i (MatVec(1, x, 0, y), matrix_square_sparse.cpp:218-242)
+__device__ __forceinline__ void spmv_row(const Arena& A, int i, const double* x, double* y) {
+  double y0 = y[3 * i + 0] * 0.0, y1 = y[3 * i + 1] * 0.0, y2 = y[3 * i + 2] * 0.0;
+  for (int s = A.row_ptr[i]; s < A.row_ptr[i + 1]; s++) {
+    const int j = A.col_idx[s];
+    const double* a = A.vcrs + 9 * (size_t)s;
+    const double x0 = x[3 * j + 0], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+    y0 += 1.0 * (a[0] * x0 + a[1] * x1 + a[2] * x2);
+    y1 += 1.0 * (a[3] * x0 + a[4] * x1 + a[5] * x2);
+    y2 += 1.0 * (a[6] * x0 + a[7] * x1 + a[8] * x2);
+  }
+  const double* a = A.vdia + 9 * (size_t)i;
+  const double x0 = x[3 * i + 0], x1 = x[3 * i + 1], x2 = x[3 * i + 2];
+  y0 += 1.0 * (a[0] * x0 + a[1] * x1 + a[2] * x2);
+  y1 += 1.0 * (a[3] * x0 + a[4] * x1 + a[5] * x2);
+  y2 += 1.0 * (a[6] * x0 + a[7] * x1 + a[8] * x2);
+  y[3 * i + 0] = y0;
+  y[3 * i + 1] = y1;
+  y[3 * i + 2] = y2;
+}
+
+// one row of DoILUDecomp (3x3 branch, ilu_sparse.cpp:507-569).  stop_here:
+// the row at which the reference gives up (updates only).  Returns 1 when the
+// pivot is singular.
+__device__ int factor_row(const Arena& A, int i, bool stop_here) {
+  double* D = A.fdia + 9 * (size_t)i;
+  for (int o = A.fac_ptr[i]; o < A.fac_ptr[i + 1]; o++) {
+    const int s = A.fac_ops[3 * o + 0], ks = A.fac_ops[3 * o + 1], tg = A.fac_ops[3 * o + 2];
+    const double* lik = A.fcrs + 9 * (size_t)s;
+    const double* ukj = A.fcrs + 9 * (size_t)ks;
+    double* dst = (tg < 0) ? D : A.fcrs + 9 * (size_t)tg;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      dst[r * 3 + 0] -= lik[r * 3 + 0] * ukj[0] + lik[r * 3 + 1] * ukj[3] + lik[r * 3 + 2] * ukj[6];
+      dst[r * 3 + 1] -= lik[r * 3 + 0] * ukj[1] + lik[r * 3 + 1] * ukj[4] + lik[r * 3 + 2] * ukj[7];
+      dst[r * 3 + 2] -= lik[r * 3 + 0] * ukj[2] + lik[r * 3 + 1] * ukj[5] + lik[r * 3 + 2] * ukj[8];
+    }
+  }
+  int singular = 0;
+  double t[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) t[k] = D[k];
+  if (fabs(det33(t)) > 1.0e-30) {
+    if (!stop_here) inv33(D, t);
+  } else {
+    singular = 1;
+  }
+  if (stop_here) return singular;
+  for (int s = A.dia_split[i]; s < A.row_ptr[i + 1]; s++) {  // U <- D^-1 U
+    double* u = A.fcrs + 9 * (size_t)s;
+    double w[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) w[k] = u[k];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+      u[r * 3 + 0] = D[r * 3 + 0] * w[0] + D[r * 3 + 1] * w[3] + D[r * 3 + 2] * w[6];
+      u[r * 3 + 1] = D[r * 3 + 0] * w[1] + D[r * 3 + 1] * w[4] + D[r * 3 + 2] * w[7];
+      u[r * 3 + 2] = D[r * 3 + 0] * w[2] + D[r * 3 + 1] * w[5] + D[r * 3 + 2] * w[8];
+    }
+  }
+  return singular;
+}
+
+__device__ void copy_matrix(const Arena& A, int v0, int v1) {
+  for (int k = 9 * v0 + threadIdx.x; k < 9 * v1; k += blockDim.x) A.fdia[k] = A.vdia[k];
+  const int s0 = A.row_ptr[v0], s1 = A.row_ptr[v1];
+  for (int k = 9 * s0 + threadIdx.x; k < 9 * s1; k += blockDim.x) A.fcrs[k] = A.vcrs[k];
+  __syncthreads();
+}
+
+// Factorises rows by level; rows after `limit` are left as copied and row
+// `limit` gets its updates only, as when the reference stops after more than
+// ten singular pivots (ilu_sparse.cpp:541-551).
+__device__ void factor_levels(const Arena& A, int inst, int limit) {
+  const int l0 = A.lev_off[inst], l1 = A.lev_off[inst + 1];
+  for (int l = l0; l < l1; l++) {
+    for (int k = A.lev_ptr[l] + threadIdx.x; k < A.lev_ptr[l + 1]; k += blockDim.x) {
+      const int i = A.lev_rows[k];
+      if (i > limit) continue;
+      A.sing[i] = factor_row(A, i, i == limit);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kSolveThreads) k_ilu_factor(Arena A, const int* list) {
+  __shared__ double sh[40];
+  __shared__ int limit;
+  const int inst = list[blockIdx.x];
+  const int v0 = A.voff[inst], v1 = A.voff[inst + 1];
+  copy_matrix(A, v0, v1);
+  factor_levels(A, inst, INT_MAX);
+  double cnt = 0;
+  for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) cnt += A.sing[i];
+  const int nsing = (int)block_sum(cnt, sh);
+  if (nsing > 10) {
+    if (threadIdx.x == 0) {
+      int seen = 0;
+      limit = v1;
+      for (int i = v0; i < v1; i++)
+        if (A.sing[i] && ++seen == 11) {
+          limit = i;
+          break;
+        }
+    }
+    __syncthreads();
+    copy_matrix(A, v0, v1);
+    factor_levels(A, inst, limit);
+  }
+  if (threadIdx.x == 0) A.st[inst].ilu_singular = nsing > 10 ? 11 : nsing;
+}
+
+// z <- (LU)^-1 z in place: forward sweep by levels, then backward sweep by
+// levels (ilu_sparse.cpp:185-215, 295-324)
+__device__ void ilu_apply(const Arena& A, int inst, double* z) {
+  for (int l = A.lev_off[inst]; l < A.lev_off[inst + 1]; l++) {
+    for (int k = A.lev_ptr[l] + threadIdx.x; k < A.lev_ptr[l + 1]; k += blockDim.x) {
+      const int i = A.lev_rows[k];
+      double t0 = z[3 * i + 0], t1 = z[3 * i + 1], t2 = z[3 * i + 2];
+      for (int s = A.row_ptr[i]; s < A.dia_split[i]; s++) {
+        const int j = A.col_idx[s];
+        const double* l9 = A.fcrs + 9 * (size_t)s;
+        const double y0 = z[3 * j + 0], y1 = z[3 * j + 1], y2 = z[3 * j + 2];
+        t0 -= l9[0] * y0 + l9[1] * y1 + l9[2] * y2;
+        t1 -= l9[3] * y0 + l9[4] * y1 + l9[5] * y2;
+        t2 -= l9[6] * y0 + l9[7] * y1 + l9[8] * y2;
+      }
+      const double* d = A.fdia + 9 * (size_t)i;
+      z[3 * i + 0] = d[0] * t0 + d[1] * t1 + d[2] * t2;
+      z[3 * i + 1] = d[3] * t0 + d[4] * t1 + d[5] * t2;
+      z[3 * i + 2] = d[6] * t0 + d[7] * t1 + d[8] * t2;
+    }
+    __syncthreads();
+  }
+  for (int l = A.blev_off[inst]; l < A.blev_off[inst + 1]; l++) {
+    for (int k = A.blev_ptr[l] + threadIdx.x; k < A.blev_ptr[l + 1]; k += blockDim.x) {
+      const int i = A.blev_rows[k];
+      double t0 = z[3 * i + 0], t1 = z[3 * i + 1], t2 = z[3 * i + 2];
+      for (int s = A.dia_split[i]; s < A.row_ptr[i + 1]; s++) {
+        const int j = A.col_idx[s];
+        const double* u = A.fcrs + 9 * (size_t)s;
+        const double y0 = z[3 * j + 0], y1 = z[3 * j + 1], y2 = z[3 * j + 2];
+        t0 -= u[0] * y0 + u[1] * y1 + u[2] * y2;
+        t1 -= u[3] * y0 + u[4] * y1 + u[5] * y2;
+        t2 -= u[6] * y0 + u[7] * y1 + u[8] * y2;
+      }
+      z[3 * i + 0] = t0;
+      z[3 * i + 1] = t1;
+      z[3 * i + 2] = t2;
+    }
+    __syncthreads();
+  }
+}
+
+// Solve_PCG (ilu_sparse.cpp:628-709) from dx = 0 with r = b
+__global__ void __launch_bounds__(kSolveThreads) k_pcg(Arena A, const int* list, double tol_in, int maxit_in) {
+  __shared__ double sh[40];
+  const int inst = list[blockIdx.x];
+  const DevParams& P = A.prm[inst];
+  const double tol = tol_in >= 0 ? tol_in : P.tol;
+  const int maxit = maxit_in >= 0 ? maxit_in : P.maxit;
+  const int v0 = A.voff[inst], v1 = A.voff[inst + 1];
+  const int d0 = 3 * v0, d1 = 3 * v1;
+  double *x = A.dx, *r = A.r, *p = A.p, *z = A.z;
+  for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) {
+    x[i] = 0.0;
+    r[i] = A.b[i];
+  }
+  __syncthreads();
+  const double s0 = cta_dot(r, r, d0, d1, sh);
+  if (s0 < 1.0e-30) {
+    if (threadIdx.x == 0) {
+      A.st[inst].solver_conv = 0.0;
+      A.st[inst].solver_iterations = 0;
+    }
+    return;
+  }
+  const double inv0 = 1.0 / s0;
+  for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) z[i] = r[i];
+  __syncthreads();
+  ilu_apply(A, inst, z);
+  for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) p[i] = z[i];
+  __syncthreads();
+  double rPr = cta_dot(r, z, d0, d1, sh);
+  for (int it = 0; it < maxit; it++) {
+    for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) spmv_row(A, i, p, z);  // Ap in z
+    __syncthreads();
+    const double pAp = cta_dot(p, z, d0, d1, sh);
+    const double alpha = rPr / pAp;
+    for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) {
+      r[i] += -alpha * z[i];
+      x[i] += +alpha * p[i];
+    }
+    __syncthreads();
+    const double sq = cta_dot(r, r, d0, d1, sh);
+    if (sq * inv0 < tol * tol) {
+      if (threadIdx.x == 0) {
+        A.st[inst].solver_conv = sqrt(sq * inv0);
+        A.st[inst].solver_iterations = it;
+      }
+      return;
+    }
+    for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) z[i] = r[i];
+    __syncthreads();
+    ilu_apply(A, inst, z);
+    const double rPr1 = cta_dot(r, z, d0, d1, sh);
+    const double beta = rPr1 / rPr;
+    rPr = rPr1;
+    for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) p[i] = z[i] + beta * p[i];
+    __syncthreads();
+  }
+  const double sq = cta_dot(r, r, d0, d1, sh);
+  if (threadIdx.x == 0) {
+    A.st[inst].solver_conv = sqrt(sq * inv0);
+    A.st[inst].solver_iterations = maxit;
+  }
+}
+
+// ---- CG over all active cloths ---------------------------------------------
+__device__ __forceinline__ double chunk_total(const double* part, int c0, int c1) {
+  double s = 0.0;
+  for (int c = c0; c < c1; c++) s += part[c];
+  return s;
+}
+
+__global__ void __launch_bounds__(kChunk) k_cg_init(Arena A, double tol_in, int maxit_in) {
+  __shared__ double sh[40];
+  const int c = blockIdx.x;
+  const int inst = A.chunk_inst[c];
+  if (!A.active[inst]) return;
+  const int row = A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk + threadIdx.x;
+  double s = 0.0;
+  if (row < A.voff[inst + 1]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double bk = A.b[3 * row + k];
+      A.dx[3 * row + k] = 0.0;
+      A.r[3 * row + k] = bk;
+      A.p[3 * row + k] = bk;
+      A.z[3 * row + k] = 0.0;
+      s += bk * bk;
+    }
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) A.part[c] = s;
+  (void)tol_in;
+  (void)maxit_in;
+}
+
+// per cloth: r.r of the start, the early exit of a tiny right-hand side
+__global__ void k_cg_start(Arena A, double tol_in, int maxit_in) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= A.ni || !A.active[inst]) return;
+  const DevParams& P = A.prm[inst];
+  const double tol = tol_in >= 0 ? tol_in : P.tol;
+  const int maxit = maxit_in >= 0 ? maxit_in : P.maxit;
+  const double s0 = chunk_total(A.part, A.chunk_lo[inst], A.chunk_hi[inst]);
+  InstState& S = A.st[inst];
+  S.sq[1] = s0;  // iteration 1 reads parity 1
+  S.solver_iterations = maxit;
+  S.solver_conv = tol;
+  if (s0 < 1.0e-30) {
+    S.done = 1;
+    S.solver_conv = 0.0;
+    S.solver_iterations = 0;
+  } else {
+    S.done = maxit <= 1 ? 1 : 0;
+    S.inv0 = 1.0 / s0;
+  }
+}
+
+// Ap = A p and the chunk partials of p.Ap
+__global__ void __launch_bounds__(kChunk) k_cg_spmv(Arena A) {
+  __shared__ double sh[40];
+  const int c = blockIdx.x;
+  const int inst = A.chunk_inst[c];
+  if (!A.active[inst] || A.st[inst].done) return;
+  const int row = A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk + threadIdx.x;
+  double s = 0.0;
+  if (row < A.voff[inst + 1]) {
+    spmv_row(A, row, A.p, A.z);
+    s = A.p[3 * row + 0] * A.z[3 * row + 0] + A.p[3 * row + 1] * A.z[3 * row + 1] +
+        A.p[3 * row + 2] * A.z[3 * row + 2];
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) A.part[c] = s;
+}
+
+// alpha = r.r / p.Ap; x += alpha p; r -= alpha Ap; chunk partials of r.r
+__global__ void __launch_bounds__(kChunk) k_cg_update(Arena A, int it) {
+  __shared__ double sh[40];
+  const int c = blockIdx.x;
+  const int inst = A.chunk_inst[c];
+  if (!A.active[inst] || A.st[inst].done) return;
+  const double pAp = chunk_total(A.part, A.chunk_lo[inst], A.chunk_hi[inst]);
+  const double alpha = A.st[inst].sq[it & 1] / pAp;
+  const int row = A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk + threadIdx.x;
+  double s = 0.0;
+  if (row < A.voff[inst + 1]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int i = 3 * row + k;
+      A.dx[i] += alpha * A.p[i];
+      const double rk = A.r[i] + (-alpha) * A.z[i];
+      A.r[i] = rk;
+      s += rk * rk;
+    }
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) A.part[A.nchunk + c] = s;
+}
+
+// convergence test, beta and p = r + beta p
+__global__ void __launch_bounds__(kChunk) k_cg_direction(Arena A, int it, double tol_in, int maxit_in) {
+  const int c = blockIdx.x;
+  const int inst = A.chunk_inst[c];
+  if (!A.active[inst] || A.st[inst].done) return;
+  const DevParams& P = A.prm[inst];
+  const double tol = tol_in >= 0 ? tol_in : P.tol;
+  InstState& S = A.st[inst];
+  const double sq = S.sq[it & 1];
+  const double sqn = chunk_total(A.part + A.nchunk, A.chunk_lo[inst], A.chunk_hi[inst]);
+  const bool first = (c == A.chunk_lo[inst]);
+  if (sqn * S.inv0 < tol * tol) {
+    if (first && threadIdx.x == 0) {
+      S.solver_conv = sqrt(sq * S.inv0);
+      S.solver_iterations = it;
+      S.done = 1;
+    }
+    return;
+  }
+  const double beta = sqn / sq;
+  const int row = A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk + threadIdx.x;
+  if (row < A.voff[inst + 1]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int i = 3 * row + k;
+      A.p[i] = A.r[i] + beta * A.p[i];
+    }
+  }
+  if (first && threadIdx.x == 0) {
+    S.sq[(it + 1) & 1] = sqn;
+    if (it + 1 >= (maxit_in >= 0 ? maxit_in : P.maxit)) S.done = 1;  // iteration cap reached
+  }
+}
+
+__global__ void k_spmv_all(Arena A, const double* x, double* y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.nv) return;
+  spmv_row(A, i, x, y);
+}
+
+}  // namespace
+
+void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_ilu_factor<<<n, kSolveThreads, 0, s>>>(A, list);
+  g_launches++;
+}
+
+void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s) {
+  if (n <= 0) return;
+  k_pcg<<<n, kSolveThreads, 0, s>>>(A, list, tol, maxit);
+  g_launches++;
+}
+
+void launch_cg_init(const Arena& A, double tol, int maxit, cudaStream_t s) {
+  k_cg_init<<<A.nchunk, kChunk, 0, s>>>(A, tol, maxit);
+  k_cg_start<<<(A.ni + 127) / 128, 128, 0, s>>>(A, tol, maxit);
+  g_launches += 2;
+}
+
+void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, cudaStream_t s) {
+  k_cg_spmv<<<A.nchunk, kChunk, 0, s>>>(A);
+  k_cg_update<<<A.nchunk, kChunk, 0, s>>>(A, it);
+  k_cg_direction<<<A.nchunk, kChunk, 0, s>>>(A, it, tol, maxit);
+  g_launches += 3;
+}
+
+void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s) {
+  k_spmv_all<<<(A.nv + 127) / 128, 128, 0, s>>>(A, x, y);
+  g_launches++;
+}
+
+}  // namespace cs

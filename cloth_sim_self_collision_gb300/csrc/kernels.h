@@ -1,0 +1,65 @@
+// kernels.h -- host launchers of the device kernels (one translation unit each
+// for assembly, solvers and collision).
+#pragma once
+#include "arena.h"
+
+namespace cs {
+
+// launches issued by this process (all contexts), for launch accounting
+extern long long g_launches;
+
+// --- assembly (k_assemble.cu) ---------------------------------------------
+void launch_quad_factors(const Arena& A, cudaStream_t s);
+// element gradients (and Hessian blocks when hess) at positions A.x; masked:
+// only cloths with A.active set
+void launch_elements(const Arena& A, bool hess, bool masked, cudaStream_t s);
+void launch_slot_reduce(const Arena& A, cudaStream_t s);
+void launch_rhs(const Arena& A, cudaStream_t s);
+void launch_update_velocity(const Arena& A, cudaStream_t s);  // masked
+void launch_finish_implicit(const Arena& A, cudaStream_t s);  // x += dx, v = dx/dt
+void launch_reintegrate(const Arena& A, cudaStream_t s);      // masked: x = x1 + v dt
+void launch_element_batch_cst(int n, const double* C, const double* c, double lambda, double myu, double* W,
+                              double* dW, double* ddW, cudaStream_t s);
+void launch_element_batch_bend(int n, const double* C, const double* c, double stiff, double* W, double* dW,
+                               double* ddW, cudaStream_t s);
+void launch_element_batch_contact(int n, const double* c, const DevParams* prm, double* W, double* dW,
+                                  double* ddW, cudaStream_t s);
+
+// --- solvers (k_solve.cu) --------------------------------------------------
+// block ILU(0) of the ILU cloths in list (device array of cloth ids)
+void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s);
+// PCG on A.b -> A.dx for the cloths in list (tol / maxit < 0: take the cloth's)
+void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s);
+// CG building blocks on all cloths with A.active set
+void launch_cg_init(const Arena& A, double tol, int maxit, cudaStream_t s);
+void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, cudaStream_t s);
+void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s);
+
+// --- collision (k_collide.cu) ------------------------------------------------
+// refit boxes of the active cloths from positions xs (and velocities vs when ccd)
+void launch_refit(const Arena& A, int ccd, const double* xs, const double* vs, double delta_override,
+                  cudaStream_t s);
+void launch_traverse(const Arena& A, const ContactBufs& C, cudaStream_t s);
+void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
+                   double delta_override, int npairs, cudaStream_t s);
+// sort + deduplicate ncand candidates into C.ce; returns via C.counters[2]
+void sort_dedupe(const Arena& A, ContactBufs& C, int ncand, cudaStream_t s);
+void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, int token,
+                     cudaStream_t s);
+void launch_riz_reset(const Arena& A, cudaStream_t s);
+// counts the in-zone vertices of each active cloth into st.riz_nodes
+void launch_riz_count(const Arena& A, cudaStream_t s);
+void launch_riz_add(const Arena& A, const ContactBufs& C, int nce, cudaStream_t s);
+// zone rigid velocities: v of zone members from snapshot v0 at positions xs
+void riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, const double* v0s, cudaStream_t s);
+int riz_count_zones(const Arena& A, ContactBufs& C, int* zone_of_vertex_dev, cudaStream_t s);
+
+size_t cub_sort_bytes(int n);
+void cub_sort_pairs(void* tmp, size_t bytes, const unsigned long long* kin, unsigned long long* kout,
+                    const int* vin, int* vout, int n, cudaStream_t s);
+void cub_sort_keys(void* tmp, size_t bytes, const unsigned long long* kin, unsigned long long* kout, int n,
+                   cudaStream_t s);
+size_t cub_scan_bytes(int n);
+void cub_exclusive_sum(void* tmp, size_t bytes, const int* in, int* out, int n, cudaStream_t s);
+
+}  // namespace cs

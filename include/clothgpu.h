@@ -1,0 +1,199 @@
+/*
+ * clothgpu.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * self_contact_sparse cloth step (implicit-Euler FEM cloth with
+ * self-collision), from the reference nobuyuki83/cloth_sim_self_collision.
+ *
+ * Plain C: opaque context handle, plain pointers and sizes, int status codes.
+ * Host arrays use the reference's layouts: positions / velocities as 3 doubles
+ * per vertex (std::vector<double> aXYZ / aUVW), triangles as 3 ints, bending
+ * stencils as 4 ints (aTri / aQuad), 3x3 blocks row-major.
+ *
+ * One context owns one CUDA device, one stream and a device arena holding any
+ * number of cloth instances ("cloths").  A cloth's topology is built once when
+ * it is added; its state (x, v) stays resident on the device between steps.
+ *
+ * Each entry point names the reference interface it replaces (file:line in the
+ * reference repository).
+ */
+#ifndef CLOTHGPU_H
+#define CLOTHGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define CS_OK 0
+#define CS_ERR_ARG 1          /* bad argument (null pointer, bad id, size)         */
+#define CS_ERR_CUDA 2         /* a CUDA call failed; see cs_last_error              */
+#define CS_ERR_NO_DEVICE 3    /* no usable GPU                                       */
+#define CS_ERR_OOM 4          /* device allocation failed                            */
+#define CS_ERR_CAPACITY 5     /* a caller-supplied output buffer is too small        */
+#define CS_ERR_TIMEOUT 6      /* a bounded device wait gave up                        */
+
+/* precision of the implicit solve */
+#define CS_PREC_FP64 0        /* plain: FP64 throughout, bit-exact with the reference */
+#define CS_PREC_MIXED 1       /* FP32 element/SpMV/CG + FP64 iterative refinement     */
+
+/* obstacle kinds (replace the penetrationDepth callback,
+ * self_contact_sparse/main.cpp:110-133) */
+#define CS_OBSTACLE_NONE 0
+#define CS_OBSTACLE_PLANE_Z 1      /* pd = obs_center[2] - z, n = (0,0,1)              */
+#define CS_OBSTACLE_SPHERE_SOLID 2 /* pd = r - |p-c|, n = (p-c)/|p-c|                   */
+#define CS_OBSTACLE_SPHERE_HOLLOW 3 /* the reference demo's inside-out sphere          */
+
+/* linear solver of the implicit step */
+#define CS_SOLVER_ILU_PCG 0   /* Solve_PCG with block ILU(0), ilu_sparse.cpp:628     */
+#define CS_SOLVER_CG 1        /* Solve_CG, matrix_square_sparse.cpp:338              */
+
+/* Parameters of one cloth: the arguments of StepTime_InternalDynamicsILU
+ * (solve_internal_sparse.h:255-275) and GetIntermidiateVelocityContactResolved
+ * (self_collision_cloth.h:21-34), plus the solver tolerance and cap that the
+ * reference hard-codes (solve_internal_sparse.h:318-319). */
+typedef struct {
+  double dt;
+  double lambda;
+  double myu;
+  double stiff_bend;
+  double gravity[3];
+  double mass_point;
+  double stiff_contact;
+  double contact_clearance;
+  double obs_center[3];
+  double obs_radius;
+  double tol;
+  int obstacle_kind;
+  int solver_kind;
+  int maxit;
+  int reserved;
+} cs_params;
+
+/* Per-frame counters of one cloth (the reference prints these,
+ * solve_internal_sparse.h:321, self_collision_cloth.cpp:386-450). */
+typedef struct {
+  int solver_iterations;
+  int n_prx;
+  int n_ccd_passes;
+  int n_ccd[5];
+  int n_riz_passes;
+  int n_riz_last;
+  int n_riz_total;
+  int riz_nodes;
+  int impulse_applied;
+  int ilu_singular;
+  double solver_conv;
+} cs_stats;
+
+typedef struct cs_ctx cs_ctx;
+
+/* ---- host-only topology (no device needed) --------------------------------- */
+/* MakeBVHTopology_TopDown (bvh_aabb.cpp:294-313): nodes[3 nnode] = parent,
+ * child0, child1 (CNodeBVH, bvh_aabb.h:18-23); node 0 is the root.  *nnode is
+ * always set; CS_ERR_CAPACITY when 3 * nnode > cap. */
+int cs_build_bvh(int np, const double *X, int nt, const int *tri, int *nodes, int cap, int *nnode);
+/* Block pattern of the implicit matrix from the bending stencils, rows sorted
+ * (CJaggedArray::SetEdgeOfElem + Sort + SetPattern, self_contact_sparse/main.cpp:578-581):
+ * row_ptr[np+1], col_idx[nb]; CS_ERR_CAPACITY when nb > cap. */
+int cs_build_pattern(int np, int nq, const int *quad, int *row_ptr, int *col_idx, int cap, int *nb);
+
+/* ---- context --------------------------------------------------------------- */
+int cs_create(int device, int precision, cs_ctx **out);
+void cs_destroy(cs_ctx *ctx);
+const char *cs_last_error(const cs_ctx *ctx);
+int cs_set_precision(cs_ctx *ctx, int precision);
+int cs_synchronize(cs_ctx *ctx);
+
+/* ---- cloths ---------------------------------------------------------------- */
+/* Adds a cloth: builds its topology on the host (matrix pattern as in
+ * self_contact_sparse/main.cpp:578-581, BVH as MakeBVHTopology_TopDown
+ * bvh_aabb.cpp:294, 1-ring as CJaggedArray::SetEdgeOfElem jagged_array.h:158)
+ * and uploads it.  State starts at x = X0, v = 0. */
+int cs_add_cloth(cs_ctx *ctx, int np, const double *X0, const int *bc, int nt, const int *tri, int nq,
+                 const int *quad, const cs_params *prm, int *id_out);
+int cs_remove_cloth(cs_ctx *ctx, int id);
+int cs_num_cloths(const cs_ctx *ctx);
+int cs_set_params(cs_ctx *ctx, int id, const cs_params *prm);
+int cs_set_state(cs_ctx *ctx, int id, const double *x, const double *v);
+int cs_get_state(cs_ctx *ctx, int id, double *x, double *v);
+int cs_get_stats(cs_ctx *ctx, int id, cs_stats *st);
+
+/* ---- whole frames -------------------------------------------------------------
+ * StepTime, self_contact_sparse/main.cpp:213-263: implicit step, contact
+ * resolution from the start-of-frame positions, re-integration and velocity
+ * update, for every cloth of the context, nsteps times. */
+int cs_step(cs_ctx *ctx, int nsteps);
+
+/* ---- stages of one cloth, host buffers in and out ------------------------------ */
+/* StepTime_InternalDynamicsILU / StepTime_InternalDynamics
+ * (solve_internal_sparse.h:255-326 / :185-253): x, v in place. */
+int cs_implicit_step(cs_ctx *ctx, int id, double *x, double *v, cs_stats *st);
+/* GetIntermidiateVelocityContactResolved, self_collision_cloth.cpp:355-456:
+ * v in place, from start-of-frame positions x1. */
+int cs_resolve_contacts(cs_ctx *ctx, int id, const double *x1, double *v, cs_stats *st);
+/* UpdateIntermidiateVelocity, solve_internal_sparse.h:329-369 */
+int cs_update_velocity(cs_ctx *ctx, int id, const double *x, double *v);
+
+/* Assembly half of StepTime_InternalDynamicsILU (solve_internal_sparse.h:276-313):
+ * the 3x3 block matrix (diagonal blocks vdia[9 np], off-diagonal vcrs[9 nb] in the
+ * pattern's order) and right-hand side b[3 np] at state (x, v).  Any output may be null. */
+int cs_assemble(cs_ctx *ctx, int id, const double *x, const double *v, double *vdia, double *vcrs,
+                double *b);
+/* Block pattern of a cloth: nb and, when non-null, row_ptr[np+1], col_idx[nb]
+ * (CMatrixSquareSparse m_colInd / m_rowPtr, matrix_square_sparse.h:40-43). */
+int cs_pattern(cs_ctx *ctx, int id, int *nb, int *row_ptr, int *col_idx);
+/* CPreconditionerILU::SetValueILU + DoILUDecomp (ilu_sparse.cpp:352-624) on the
+ * last assembled matrix; factor blocks out (nullable) and the singular-pivot count. */
+int cs_ilu_factor(cs_ctx *ctx, int id, double *fdia, double *fcrs, int *nsing);
+/* Solve_PCG (ilu_sparse.cpp:628-709) on the last assembled matrix and factor. */
+int cs_solve_pcg(cs_ctx *ctx, int id, const double *b, double tol, int maxit, double *x, double *conv,
+                 int *iter);
+/* Solve_CG (matrix_square_sparse.cpp:338-406) on the last assembled matrix. */
+int cs_solve_cg(cs_ctx *ctx, int id, const double *b, double tol, int maxit, double *x, double *conv,
+                int *iter);
+/* CMatrixSquareSparse::MatVec(1, x, 0, y) (matrix_square_sparse.cpp:167-270) */
+int cs_spmv(cs_ctx *ctx, int id, const double *x, double *y);
+
+/* BVH of a cloth: nnode and, when non-null, nodes[3 nnode] = parent, child0,
+ * child1 (CNodeBVH, bvh_aabb.h:18-23; child1 == -1 marks a leaf). */
+int cs_bvh_nodes(cs_ctx *ctx, int id, int *nnode, int *nodes);
+/* BuildBoundingBoxChild_Prx / _CCD (bvh_aabb.cpp:23-106): boxes[7 nnode] =
+ * xmin, xmax, ymin, ymax, zmin, zmax, non-empty flag.  boxes may be null. */
+int cs_refit_prx(cs_ctx *ctx, int id, const double *x, double delta, double *boxes);
+int cs_refit_ccd(cs_ctx *ctx, int id, const double *x, const double *v, double dt, double *boxes);
+/* GetContactElement_Proximity / _CCD (bvh_aabb.cpp:441-557, 797-923) after the
+ * matching refit: contacts in std::set order, 5 ints each (is_fv, ino0..ino3),
+ * up to cap; *n receives the full count (CS_ERR_CAPACITY if it exceeds cap). */
+int cs_contacts_prx(cs_ctx *ctx, int id, const double *x, double delta, int *out, int cap, int *n);
+int cs_contacts_ccd(cs_ctx *ctx, int id, const double *x, const double *v, double dt, double delta,
+                    int *out, int cap, int *n);
+/* SelfCollisionImpulse_Proximity / _CCD (self_collision_cloth.cpp:20-212):
+ * sequential-order impulses over a contact list, v in place. */
+int cs_impulse_prx(cs_ctx *ctx, int id, const double *x, double *v, const int *ce, int n);
+int cs_impulse_ccd(cs_ctx *ctx, int id, const double *x, double *v, const int *ce, int n);
+/* MakeRigidImpactZone / ApplyRigidImpactZone (self_collision_cloth.cpp:220-348):
+ * reset the zones, add contacts, read zone ids per vertex (-1 outside; ids are
+ * an arbitrary labelling of the same partition), apply the rigid velocities. */
+int cs_riz_reset(cs_ctx *ctx, int id);
+int cs_riz_add(cs_ctx *ctx, int id, const int *ce, int n);
+int cs_riz_zones(cs_ctx *ctx, int id, int *zone_of_vertex, int *nzone);
+int cs_riz_apply(cs_ctx *ctx, int id, const double *x, double *v, const double *v0);
+
+/* ---- element kernels on batches (cloth_internal_physics.h) --------------------- */
+/* WdWddW_CST (:70-176) for n triangles: C, c [n][9]; W[n], dW[n][9], ddW[n][81] */
+int cs_element_cst(cs_ctx *ctx, int n, const double *C, const double *c, double lambda, double myu,
+                   double *W, double *dW, double *ddW);
+/* WdWddW_Bend (:180-238) for n stencils: C, c [n][12]; W[n], dW[n][12], ddW[n][144] */
+int cs_element_bend(cs_ctx *ctx, int n, const double *C, const double *c, double stiff, double *W,
+                    double *dW, double *ddW);
+/* WdWddW_Contact (:243-280) for n points against the obstacle of prm */
+int cs_element_contact(cs_ctx *ctx, int n, const double *c, const cs_params *prm, double *W, double *dW,
+                       double *ddW);
+
+/* ---- counters ------------------------------------------------------------------ */
+/* Kernel launches issued by this context since creation (for launch accounting). */
+long long cs_launch_count(const cs_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

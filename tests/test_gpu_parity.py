@@ -1,0 +1,223 @@
+"""Parity of the CUDA library (through its C ABI) with the oracle, FP64 mode.
+
+Tolerances: every stage whose arithmetic is a fixed sequence of IEEE double
+operations is compared bit for bit (element kernels, assembly, ILU factor,
+refits, contact sets, impulses, impact zones, velocity update).  The Krylov
+solves sum inner products as a tree instead of one running sum, so their
+results (and anything downstream of them) are compared with
+    max |gpu - oracle| <= RTOL * max(1, max |oracle|),   RTOL = 1e-9.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from cloth_sim_self_collision_gb300 import scene
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def close(a, b, rtol=RTOL):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return a.shape == b.shape and np.max(np.abs(a - b), initial=0.0) <= rtol * max(1.0, np.max(np.abs(b), initial=0.0))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from cloth_sim_self_collision_gb300 import build
+    build.build()
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    c = ClothContext()
+    yield c
+    c.close()
+
+
+def fold_scene():
+    return scene.square_cloth(31, 1.0, 0.4, sphere_radius=0.2, clearance=0.01, seed=11,
+                              solver_kind=scene.SOLVER_CG, tol=1.0e-6, maxit=1000)
+
+
+def scene_for(name):
+    return scene.config_small() if name == "small_21" else fold_scene()
+
+
+def load(name):
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        meta = json.load(f)
+    return meta, dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def test_elements_bit_exact(ctx, oracle_port):
+    g = dict(np.load(os.path.join(GOLDEN, "elements.npz")))
+    inp, out = g["cst_in"], g["cst_out"]
+    for lam_myu in {(r[18], r[19]) for r in inp}:
+        sel = [k for k, r in enumerate(inp) if (r[18], r[19]) == lam_myu]
+        W, dW, ddW = ctx.element_cst(inp[sel, :9], inp[sel, 9:18], *lam_myu)
+        assert np.array_equal(np.concatenate([W[:, None], dW, ddW], axis=1), out[sel])
+    inp, out = g["bend_in"], g["bend_out"]
+    for k in range(inp.shape[0]):
+        W, dW, ddW = ctx.element_bend(inp[k:k + 1, :12], inp[k:k + 1, 12:24], inp[k, 24])
+        assert np.array_equal(np.concatenate([W, dW[0], ddW[0]]), out[k])
+    rng = np.random.default_rng(5)
+    C = rng.uniform(-1, 1, (500, 9))
+    c = C + rng.normal(0, 0.3, (500, 9))
+    W, dW, ddW = ctx.element_cst(C, c, 1.0, 1.0)
+    for k in range(0, 500, 7):
+        w, dw, ddw = O.wdwddw_cst(oracle_port, C[k], c[k], 1.0, 1.0)
+        assert W[k] == w and np.array_equal(dW[k], dw) and np.array_equal(ddW[k], ddw)
+    prm = scene.Params(obs_radius=0.3)
+    p = rng.uniform(-0.35, 0.35, (300, 3))
+    W, dW, ddW = ctx.element_contact(p, prm)
+    for k in range(300):
+        w, dw, ddw = O.wdwddw_contact(oracle_port, p[k], prm)
+        assert W[k] == w and np.array_equal(dW[k], dw) and np.array_equal(ddW[k], ddw)
+
+
+@pytest.mark.parametrize("name", ["small_21", "fold_31"])
+def test_topology(ctx, name):
+    _, arr = load(name)
+    cid = ctx.add_cloth(scene_for(name))
+    assert np.array_equal(ctx.bvh_nodes(cid), arr["bvh_nodes"])
+    rp, ci = ctx.pattern(cid)
+    assert np.array_equal(rp, arr["row_ptr"]) and np.array_equal(ci, arr["col_idx"])
+    ctx.remove_cloth(cid)
+
+
+@pytest.mark.parametrize("name", ["small_21", "fold_31"])
+def test_stages_at_probe_frame(ctx, oracle_port, name):
+    meta, arr = load(name)
+    c = scene_for(name)
+    prm = c.params
+    cid = ctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    x, v = arr["probe_x"], arr["probe_v"]
+    # assembly and factor: bit-exact
+    a = ctx.assemble(cid, x, v)
+    b = orc.assemble(x, v)
+    for u, w in zip(a, b):
+        assert np.array_equal(u, w)
+    rhs = b[2]
+    if prm.solver_kind == scene.SOLVER_ILU_PCG:
+        fa = ctx.ilu(cid)
+        fb = orc.ilu()
+        assert np.array_equal(fa[0], fb[0]) and np.array_equal(fa[1], fb[1]) and fa[2] == fb[2]
+        xa, ca, ia = ctx.pcg(cid, rhs, 1e-6, 100)
+        xb, cb, ib = orc.pcg(rhs, 1e-6, 100)
+        assert ia == ib and close(xa, xb) and abs(ca - cb) <= 1e-6 * cb + 1e-300
+    xa, ca, ia = ctx.cg(cid, rhs, 1e-6, 1000)
+    xb, cb, ib = orc.cg(rhs, 1e-6, 1000)
+    assert abs(ia - ib) <= 1 and close(xa, xb, 1e-7)
+    # spmv against a dense restatement of the blocks
+    rp, ci = ctx.pattern(cid)
+    y = ctx.spmv(cid, xb)
+    vd, vc = b[0].reshape(-1, 3, 3), b[1].reshape(-1, 3, 3)
+    X = xb.reshape(-1, 3)
+    ref = np.einsum("nij,nj->ni", vd, X)
+    for i in range(c.np):
+        for s in range(rp[i], rp[i + 1]):
+            ref[i] += vc[s] @ X[ci[s]]
+    assert close(y, ref.reshape(-1), 1e-12)
+    # implicit step
+    x1a, v1a, sa = ctx.implicit(cid, x, v)
+    x1b, v1b, sb = orc.implicit(x, v)
+    assert close(x1a, x1b) and close(v1a, v1b, 1e-7)
+    assert abs(sa["solver_iterations"] - sb["solver_iterations"]) <= 1
+    # collision stages from identical inputs: bit-exact
+    assert np.array_equal(ctx.refit_prx(cid, x, prm.contact_clearance), orc.refit_prx(x, prm.contact_clearance))
+    assert np.array_equal(ctx.refit_ccd(cid, x, x1b, prm.dt), orc.refit_ccd(x, x1b, prm.dt))
+    prx = ctx.contacts_prx(cid, x, prm.contact_clearance)
+    assert np.array_equal(prx, arr["contacts_prx"])
+    ccd = ctx.contacts_ccd(cid, x, v1b, prm.dt, prm.contact_clearance)
+    assert np.array_equal(ccd, orc.contacts_ccd(x, v1b, prm.dt, prm.contact_clearance))
+    vi = ctx.impulse_prx(cid, x, v1b, prx)
+    assert np.array_equal(vi, orc.impulse_prx(x, v1b, prx))
+    ccd2 = ctx.contacts_ccd(cid, x, vi, prm.dt, prm.contact_clearance)
+    assert np.array_equal(ccd2, arr["contacts_ccd_after_prx"])
+    assert np.array_equal(ctx.impulse_ccd(cid, x, vi, ccd2), orc.impulse_ccd(x, vi, ccd2))
+    ctx.riz_reset(cid)
+    ctx.riz_add(cid, ccd2)
+    za, nza = ctx.riz_zones(cid)
+    zb = arr["riz_zones"]
+    assert nza == meta["probe"]["riz_count"]
+    # same partition: a bijection between labels
+    pairs = {(p, q) for p, q in zip(za.tolist(), zb.tolist())}
+    assert len(pairs) == len({p for p, _ in pairs}) == len({q for _, q in pairs})
+    assert all((p < 0) == (q < 0) for p, q in pairs)
+    orc.riz_reset()
+    orc.riz_add(ccd2)
+    assert np.array_equal(ctx.riz_apply(cid, x, vi, vi), orc.riz_apply(x, vi, vi))
+    vr_a, st_a = ctx.resolve(cid, x, v1b)
+    vr_b, st_b = orc.resolve(x, v1b)
+    assert np.array_equal(vr_a, vr_b)
+    for k in ("n_prx", "n_ccd_passes", "n_ccd", "n_riz_passes", "n_riz_last", "n_riz_total", "riz_nodes",
+              "impulse_applied"):
+        assert st_a[k] == st_b[k], k
+    assert np.array_equal(ctx.update_velocity(cid, x1b, vr_b), orc.update_velocity(x1b, vr_b))
+    ctx.remove_cloth(cid)
+
+
+@pytest.mark.parametrize("name,frames", [("small_21", [0, 36, 40, 45, 47, 89, 90, 160, 190]),
+                                         ("fold_31", [30, 35, 37, 38, 40, 50, 60, 100])])
+def test_one_step_from_oracle_states(ctx, oracle_port, name, frames):
+    """One GPU frame from oracle states at contact-rich frames against the oracle's next frame."""
+    c = scene_for(name)
+    cid = ctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    frame = 0
+    for f in frames:
+        orc.step(f - frame)
+        frame = f
+        ctx.set_state(cid, orc.x, orc.v)
+        nxt = O.OracleCloth(oracle_port, c)
+        nxt.x, nxt.v = orc.x.copy(), orc.v.copy()
+        sb = nxt.step(1)[0]
+        ctx.step(1)
+        xa, va = ctx.get_state(cid)
+        sa = ctx.stats(cid)
+        assert close(xa, nxt.x), (name, f, np.abs(xa - nxt.x).max())
+        assert close(va, nxt.v, 1e-7), (name, f, np.abs(va - nxt.v).max())
+        for k in ("n_prx", "n_ccd_passes", "n_riz_passes", "impulse_applied"):
+            assert sa[k] == sb[k], (name, f, k, sa[k], sb[k])
+        nxt.close()
+    ctx.remove_cloth(cid)
+
+
+def test_trajectory_small(ctx, oracle_port):
+    """300 frames of the 21x21 sheet: positions within RTOL of the oracle at every frame."""
+    c = scene.config_small()
+    cid = ctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    worst = 0.0
+    for f in range(300):
+        orc.step(1)
+        ctx.step(1)
+        xa, _ = ctx.get_state(cid)
+        err = np.abs(xa - orc.x).max() / max(1.0, np.abs(orc.x).max())
+        worst = max(worst, err)
+        assert err <= RTOL, (f, err)
+    ctx.remove_cloth(cid)
+
+
+def test_batch_matches_single(ctx, oracle_port):
+    """Cloths stepped together in one arena give the same result as alone."""
+    cl = scene.config_batch(count=5)
+    ids = [ctx.add_cloth(c) for c in cl]
+    ctx.step(3)
+    together = [ctx.get_state(i)[0] for i in ids]
+    for i in ids:
+        ctx.remove_cloth(i)
+    for c, xt in zip(cl, together):
+        i = ctx.add_cloth(c)
+        ctx.step(3)
+        xs, _ = ctx.get_state(i)
+        assert np.array_equal(xs, xt)
+        ctx.remove_cloth(i)
+        orc = O.OracleCloth(oracle_port, c)
+        orc.step(3)
+        assert close(xs, orc.x)
