@@ -1,0 +1,358 @@
+"""Benchmark of the self_contact_sparse cloth step on GB300.
+
+Workload (one "step" = one frame of every cloth): 512 independent square
+cloths in one device arena, grid side uniform in 11..81 vertices (1.3 M
+vertices in total), 1 m sheets dropped from 0.3-1.5 m onto spheres of radius
+0.1-0.4 m, rotated about z, material lambda = mu = 1, bending 1e-3, dt 0.02,
+clearance 0.01, CG tolerance 1e-6 (the reference's Solve_CG: ILU(0) meets
+non-positive pivots on the finer sheets).  Inputs are synthetic and seeded.
+
+Metric: vertex-steps/s (cloth vertices advanced one frame per second, whole
+job), with p50 / p99 frame latency.  `value` is timed with CUDA events on the
+library's stream with the state resident in HBM; `e2e` goes through the C ABI
+with the state copied from pinned host memory and back every frame.
+
+    python bench.py [--steps K] [--warmup W] [--impl native|reference] [--cloths N]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "vertex-steps/s batched vs plain GPU path at 1e-6 err; p50/p99 step latency"
+UNIT = "vertex-steps/s"
+
+
+def workload_config(n_cloths: int, nv: int, precision: str) -> dict:
+    return {
+        "workload": f"{n_cloths} cloths in one arena, grid side U{{11..81}} (1 m), drop 0.3-1.5 m onto "
+                    f"spheres r 0.1-0.4 m, CG tol 1e-6, dt 0.02",
+        "cloths": n_cloths,
+        "vertices": nv,
+        "precision": precision,
+        "l2": "inputs larger than L2 (FP64 block matrix of the arena > 1 GB)",
+    }
+
+
+def read_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return {"hbm_gbs": float(p["hbm_gbs"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------------------
+# algorithmic bytes of the kernels we report a roofline for (FP64 values 8 B, indices 4 B)
+# SpMV over a cloth of N vertices and B off-diagonal blocks: blocks + column indices,
+# diagonal blocks, x read, y written, row pointers.
+def spmv_bytes(nv: int, nb: int, s: int = 8) -> int:
+    return nb * (9 * s + 4) + nv * (9 * s + 6 * s + 4)
+
+
+def run_cpu_baseline(cloths, budget_s: float = 12.0) -> dict:
+    """The oracle restatement (single core) on a bounded sample of the workload."""
+    from oracle import oracle as O
+    O.build("port")
+    lib = O.OracleLib("port")
+    done_vs, t_used, frames = 0, 0.0, 0
+    used = 0
+    for c in cloths:
+        sim = O.OracleCloth(lib, c)
+        t0 = time.perf_counter()
+        sim.step(2)
+        dt = time.perf_counter() - t0
+        t_used += dt
+        done_vs += 2 * c.np
+        frames += 2
+        used += 1
+        sim.close()
+        if t_used > budget_s:
+            break
+    return {"value": done_vs / t_used, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle restatement, first {used} cloths of the workload x 2 frames each "
+                      f"({done_vs} vertex-steps in {t_used:.1f} s), 1 host core"}
+
+
+# --------------------------------------------------------------------------------------
+def native(args):
+    import torch
+
+    from cloth_sim_self_collision_gb300 import build as B
+    from cloth_sim_self_collision_gb300 import scene
+    from cloth_sim_self_collision_gb300.context import ClothContext
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    B.build()
+    torch.cuda.set_device(local)
+    cloths = scene.config_batch(count=args.cloths)
+    ctx = ClothContext(local, "fp64")
+    ids = [ctx.add_cloth(c) for c in cloths]
+    nv = ctx.num_vertices()
+    nb_total = 0
+    for i in ids:
+        rp, _ = ctx.pattern(i)
+        nb_total += int(rp[-1])
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # warm-up (also builds and uploads the arena)
+    ctx.step(args.warmup)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+
+    # timed region: K frames, resident state, per-frame events on the library's stream
+    launches0 = ctx.launch_count()
+    ctx.profile(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    iters = []
+    for k in range(args.steps):
+        ctx.step(1)
+        ev[k + 1].record(stream)
+        iters.append(sum(ctx.stats(i)["solver_iterations"] for i in ids[:1]))
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = sum(step_ms)
+    prof = {}
+    for name in ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit",
+                 "traverse", "narrow", "impulse", "pcg", "ilu_factor"):
+        prof[name] = ctx.profile_read(name)
+    ctx.profile(False)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * nv * args.steps / (total_ms / 1e3)
+
+    # roofline of the dominant kernel class
+    top = max(prof, key=lambda k: prof[k][0])
+    peaks = read_peaks()
+    roof = {"kernel": top, "bound": "hbm", "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "peak_source": peaks["source"], "traffic": None}
+    ms, n = prof[top]
+    roof["launches"] = n
+    roof["avg_launch_us"] = 1e3 * ms / max(n, 1)
+    if top == "cg_spmv":
+        # every launch covers the rows of the cloths whose CG has not converged;
+        # bound from above by the whole arena per launch
+        per_launch = spmv_bytes(nv, nb_total)
+        roof["achieved"] = per_launch / (ms / max(n, 1) / 1e3) / 1e9
+        roof["bytes_per_launch"] = per_launch
+        roof["bytes_note"] = "whole-arena SpMV bytes; launches late in the solve skip converged cloths"
+    else:
+        roof["achieved"] = None
+    if roof["achieved"] is not None:
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    else:
+        roof["frac"] = None
+
+    # end to end through the C ABI: pinned host state in, frame, state out
+    xs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
+    vs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
+    ctx.get_states(xs.numpy(), vs.numpy())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.set_states(xs.numpy(), vs.numpy())
+        ctx.step(1)
+        ctx.get_states(xs.numpy(), vs.numpy())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e = {"value": world * nv * args.steps / (e2e_ms / 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": 2 * 3 * nv * 8, "d2h_bytes_per_step": 2 * 3 * nv * 8}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(len(cloths), nv, "fp64 (plain path; one arena, one launch sequence per frame)"),
+        "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+        "e2e": e2e, "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
+        "kernel_ms": {k: round(v[0], 3) for k, v in prof.items()},
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = run_cpu_baseline(cloths)
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------------------
+_W = {}
+
+
+def _ref_init(lib_kind, cloth_args):
+    from cloth_sim_self_collision_gb300 import scene
+    from oracle import oracle as O
+    lib = O.OracleLib(lib_kind)
+    allc = scene.config_batch(count=cloth_args[0])
+    _W["sims"] = [O.OracleCloth(lib, allc[i]) for i in cloth_args[1]]
+
+
+def _ref_step(_):
+    t0 = time.perf_counter()
+    n = 0
+    for s in _W["sims"]:
+        s.step(1)
+        n += s.n
+    return n, time.perf_counter() - t0
+
+
+def reference(args):
+    """The reference's CPU path on the host cores: the reference build where it
+    exists on this machine, else the oracle restatement; cloths spread over all
+    cores, one frame of each per step."""
+    import multiprocessing as mp
+
+    from oracle import oracle as O
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    kind = "reference" if O.ref_available() else "port"
+    lib_kind = "ref" if kind == "reference" else "port"
+    if kind == "port":
+        O.build("port")
+    cores = os.cpu_count() or 1
+    n = args.ref_cloths
+    groups = [list(range(w, n, cores)) for w in range(cores)]
+    groups = [g for g in groups if g]
+    ctx = mp.get_context("spawn")
+    pools = [ctx.Pool(1, initializer=_ref_init, initargs=(lib_kind, (args.cloths, g))) for g in groups]
+    try:
+        def one_step():
+            t0 = time.perf_counter()
+            res = [p.apply_async(_ref_step, (0,)) for p in pools]
+            out = [r.get() for r in res]
+            return sum(o[0] for o in out), time.perf_counter() - t0
+
+        for _ in range(args.warmup):
+            one_step()
+        vs, t = 0, 0.0
+        step_s = []
+        for _ in range(args.steps):
+            a, b = one_step()
+            vs += a
+            t += b
+            step_s.append(b)
+    finally:
+        for p in pools:
+            p.terminate()
+    value = vs / t
+    sample = (f"{n} of the workload's cloths, one frame each per step, spread over {len(groups)} processes "
+              f"on {cores} host cores ({'reference sources' if kind == 'reference' else 'oracle restatement'})")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args.cloths, None, "fp64 (CPU)"),
+        "p50_step_ms": 1e3 * float(np.percentile(step_s, 50)), "p99_step_ms": 1e3 * float(np.percentile(step_s, 99)),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(groups), "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--cloths", type=int, default=512)
+    ap.add_argument("--ref-cloths", type=int, default=512)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 0 or args.steps < 1:
+        raise SystemExit("need --steps >= 1 and --warmup >= 0")
+    if args.impl == "reference":
+        reference(args)
+    else:
+        native(args)
+
+
+if __name__ == "__main__":
+    main()

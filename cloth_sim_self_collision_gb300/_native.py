@@ -22,6 +22,8 @@ CS_ERR_OOM = 4
 CS_ERR_CAPACITY = 5
 CS_ERR_TIMEOUT = 6
 
+CS_FLAG_EXACT_DOTS = 1
+
 CS_PREC_FP64 = 0
 CS_PREC_MIXED = 1
 
@@ -33,7 +35,8 @@ EXPORTS = [
     "cs_ilu_factor", "cs_solve_pcg", "cs_solve_cg", "cs_spmv", "cs_bvh_nodes", "cs_refit_prx", "cs_refit_ccd",
     "cs_contacts_prx", "cs_contacts_ccd", "cs_impulse_prx", "cs_impulse_ccd", "cs_riz_reset", "cs_riz_add",
     "cs_riz_zones", "cs_riz_apply", "cs_element_cst", "cs_element_bend", "cs_element_contact",
-    "cs_launch_count", "cs_build_bvh", "cs_build_pattern",
+    "cs_launch_count", "cs_build_bvh", "cs_build_pattern", "cs_set_states", "cs_get_states", "cs_num_vertices",
+    "cs_profile", "cs_profile_read", "cs_stream",
 ]
 
 
@@ -51,7 +54,7 @@ class CsParams(ctypes.Structure):
         ("contact_clearance", ctypes.c_double), ("obs_center", ctypes.c_double * 3),
         ("obs_radius", ctypes.c_double), ("tol", ctypes.c_double),
         ("obstacle_kind", ctypes.c_int), ("solver_kind", ctypes.c_int),
-        ("maxit", ctypes.c_int), ("reserved", ctypes.c_int),
+        ("maxit", ctypes.c_int), ("flags", ctypes.c_int),
     ]
 
     @classmethod
@@ -63,6 +66,7 @@ class CsParams(ctypes.Structure):
         c.obs_center[:] = list(p.obs_center)
         c.obs_radius, c.tol = p.obs_radius, p.tol
         c.obstacle_kind, c.solver_kind, c.maxit = p.obstacle_kind, p.solver_kind, p.maxit
+        c.flags = getattr(p, "flags", 0)
         return c
 
 
@@ -145,6 +149,12 @@ def load(path: str | None = None, build_if_missing: bool = False):
     f("cs_launch_count", ctypes.c_longlong, _V)
     f("cs_build_bvh", i, i, _D, i, _I, _I, i, _I)
     f("cs_build_pattern", i, i, i, _I, _I, _I, i, _I)
+    f("cs_set_states", i, _V, _D, _D)
+    f("cs_get_states", i, _V, _D, _D)
+    f("cs_num_vertices", ctypes.c_longlong, _V)
+    f("cs_profile", i, _V, i)
+    f("cs_stream", _V, _V)
+    f("cs_profile_read", i, _V, ctypes.c_char_p, _D, ctypes.POINTER(ctypes.c_longlong))
     _lib = L
     return L
 

@@ -93,6 +93,29 @@ class ClothContext:
     def launch_count(self) -> int:
         return int(self.L.cs_launch_count(self.h))
 
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(self.L.cs_stream(self.h) or 0)
+
+    def num_vertices(self) -> int:
+        return int(self.L.cs_num_vertices(self.h))
+
+    def set_states(self, x=None, v=None):
+        """States of all cloths, back to back in the order they were added."""
+        self._ck(self.L.cs_set_states(self.h, None if x is None else N.dp(x), None if v is None else N.dp(v)))
+
+    def get_states(self, x, v):
+        self._ck(self.L.cs_get_states(self.h, None if x is None else N.dp(x), None if v is None else N.dp(v)))
+
+    def profile(self, enable: bool):
+        self._ck(self.L.cs_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self, kernel: str):
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        self._ck(self.L.cs_profile_read(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
     # ---- stages (host arrays in / out) -------------------------------------------
     def implicit(self, cid, x, v):
         """StepTime_InternalDynamicsILU / StepTime_InternalDynamics (solve_internal_sparse.h:185-326)."""

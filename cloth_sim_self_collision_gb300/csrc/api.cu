@@ -397,11 +397,16 @@ void run_cg(cs_ctx* c, const std::vector<int>& cg, double tol, int maxit) {
   const Arena& A = c->A;
   set_active(c, cg);
   int cap = 0;
+  bool serial = false;
   for (int i = 0; i < A.ni; i++)
-    if (cg[i]) cap = std::max(cap, maxit >= 0 ? maxit : c->cloths[c->order[i]]->prm.maxit);
+    if (cg[i]) {
+      const cs_params& p = c->cloths[c->order[i]]->prm;
+      cap = std::max(cap, maxit >= 0 ? maxit : p.maxit);
+      serial |= (p.flags & CS_FLAG_EXACT_DOTS) != 0;
+    }
   launch_cg_init(A, tol, maxit, c->stream);
   for (int it = 1; it < cap; it++) {
-    launch_cg_iteration(A, it, tol, maxit, c->stream);
+    launch_cg_iteration(A, it, tol, maxit, serial, c->stream);
     if (it % 8 == 0) {
       pull_states(c);
       bool all = true;
@@ -680,6 +685,8 @@ void cs_destroy(cs_ctx* c) {
 }
 
 const char* cs_last_error(const cs_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+void* cs_stream(const cs_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int cs_set_precision(cs_ctx* c, int precision) {
   return guarded(c, [&] {
@@ -1214,6 +1221,49 @@ int cs_element_contact(cs_ctx* c, int n, const double* cc, const cs_params* prm,
 }
 
 long long cs_launch_count(const cs_ctx* c) { return c ? g_launches - c->launches0 : 0; }
+
+int cs_profile(cs_ctx* c, int enable) {
+  return guarded(c, [&] {
+    CK(cudaStreamSynchronize(c->stream));
+    prof_reset();
+    prof_enable(enable != 0);
+  });
+}
+
+int cs_profile_read(cs_ctx* c, const char* kernel, double* total_ms, long long* launches) {
+  return guarded(c, [&] {
+    if (!kernel) throw ArgError("null kernel name");
+    CK(cudaStreamSynchronize(c->stream));
+    if (!prof_read(kernel, total_ms, launches)) throw ArgError(std::string("unknown kernel class ") + kernel);
+  });
+}
+
+int cs_set_states(cs_ctx* c, const double* x, const double* v) {
+  return guarded(c, [&] {
+    ensure(c);
+    const size_t n = 3 * (size_t)c->A.nv;
+    if (x) up(c, c->A.x, x, n);
+    if (v) up(c, c->A.v, v, n);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_get_states(cs_ctx* c, double* x, double* v) {
+  return guarded(c, [&] {
+    ensure(c);
+    const size_t n = 3 * (size_t)c->A.nv;
+    if (x) down(c, x, c->A.x, n);
+    if (v) down(c, v, c->A.v, n);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+long long cs_num_vertices(const cs_ctx* c) {
+  if (!c) return 0;
+  long long n = 0;
+  for (auto& kv : c->cloths) n += kv.second->topo.np;
+  return n;
+}
 
 int cs_build_bvh(int np, const double* X, int nt, const int* tri, int* nodes, int cap, int* nnode) {
   if (np <= 0 || nt <= 0 || !X || !tri) return CS_ERR_ARG;

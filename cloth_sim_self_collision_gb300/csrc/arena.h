@@ -16,7 +16,7 @@ struct DevParams {
   double mass_point, stiff_contact, contact_clearance;
   double obs_center[3];
   double obs_radius, tol;
-  int obstacle_kind, solver_kind, maxit, reserved;
+  int obstacle_kind, solver_kind, maxit, flags;
 };
 
 // contact element as produced by the narrow phase
@@ -41,6 +41,7 @@ struct InstState {
   double sq[2];      // CG: r.r of the previous / current iteration (by parity)
   double inv0;
   double rpr;        // PCG: r.Pr
+  double dot[2];     // CG with serial inner products: p.Ap, r.r of this iteration
 };
 
 struct Arena {

@@ -292,7 +292,9 @@ void launch_quad_factors(const Arena& A, cudaStream_t s) {
 }
 
 void launch_elements(const Arena& A, bool hess, bool masked, cudaStream_t s) {
+  prof_begin(PK_TRI_ELEMENTS, s);
   k_tri_elements<<<blocks_for(A.nt), kThreads, 0, s>>>(A, hess ? 1 : 0, masked ? 1 : 0);
+  prof_end(PK_TRI_ELEMENTS, s);
   g_launches++;
   if (A.nq) {
     k_quad_grad<<<blocks_for(A.nq), kThreads, 0, s>>>(A, masked ? 1 : 0);
@@ -301,12 +303,16 @@ void launch_elements(const Arena& A, bool hess, bool masked, cudaStream_t s) {
 }
 
 void launch_slot_reduce(const Arena& A, cudaStream_t s) {
+  prof_begin(PK_SLOT_REDUCE, s);
   k_slot_reduce<<<blocks_for(A.nb + A.nv), kThreads, 0, s>>>(A);
+  prof_end(PK_SLOT_REDUCE, s);
   g_launches++;
 }
 
 void launch_rhs(const Arena& A, cudaStream_t s) {
+  prof_begin(PK_RHS, s);
   k_rhs<<<blocks_for(A.nv), kThreads, 0, s>>>(A);
+  prof_end(PK_RHS, s);
   g_launches++;
 }
 

@@ -658,19 +658,25 @@ __global__ void k_riz_labels(Arena A, int* zone_of) {
 void launch_refit(const Arena& A, int ccd, const double* xs, const double* vs, double delta_override,
                   cudaStream_t s) {
   cudaMemsetAsync(A.refit_cnt, 0, sizeof(int) * (size_t)A.nn, s);
+  prof_begin(PK_REFIT, s);
   k_refit<<<nblk(A.nt), kT, 0, s>>>(A, ccd, xs, vs, delta_override);
+  prof_end(PK_REFIT, s);
   g_launches++;
 }
 
 void launch_traverse(const Arena& A, const ContactBufs& C, cudaStream_t s) {
+  prof_begin(PK_TRAVERSE, s);
   k_traverse<<<nblk(A.nt), kT, 0, s>>>(A, C);
+  prof_end(PK_TRAVERSE, s);
   g_launches++;
 }
 
 void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
                    double delta_override, int npairs, cudaStream_t s) {
   if (npairs <= 0) return;
+  prof_begin(PK_NARROW, s);
   k_narrow<<<nblk(npairs), kT, 0, s>>>(A, C, ccd, xs, vs, delta_override, npairs);
+  prof_end(PK_NARROW, s);
   g_launches++;
 }
 
@@ -724,8 +730,10 @@ void sort_dedupe(const Arena& A, ContactBufs& C, int n, cudaStream_t s) {
 
 void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, int token,
                      cudaStream_t s) {
+  prof_begin(PK_IMPULSE, s);
   k_impulse_levels<<<nblk(A.ni, 32), 32, 0, s>>>(A, C, token);
   k_impulse_apply<<<A.ni, 128, 0, s>>>(A, C, ccd, xs, vs);
+  prof_end(PK_IMPULSE, s);
   g_launches += 2;
 }
 

@@ -57,11 +57,29 @@ __device__ double block_sum(double v, double* sh) {
   return sh[32];
 }
 
-// <a, b> over dofs [lo, hi) of a cloth, by one CTA
-__device__ double cta_dot(const double* a, const double* b, int lo, int hi, double* sh) {
+// <a, b> over dofs [lo, hi) of a cloth, by one CTA: a deterministic tree sum,
+// or with `serial` one running sum in dof order like the reference's
+// InnerProduct (matrix_square_sparse.cpp:313-325)
+__device__ double cta_dot(const double* a, const double* b, int lo, int hi, double* sh, bool serial) {
+  if (serial) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double r = 0.0;
+      for (int i = lo; i < hi; i++) r += a[i] * b[i];
+      sh[33] = r;
+    }
+    __syncthreads();
+    return sh[33];
+  }
   double s = 0.0;
   for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) s += a[i] * b[i];
   return block_sum(s, sh);
+}
+
+__device__ __forceinline__ double serial_dot(const double* a, const double* b, int lo, int hi) {
+  double r = 0.0;
+  for (int i = lo; i < hi; i++) r += a[i] * b[i];
+  return r;
 }
 
 // y_i = 0 * y_i + sum_j A_ij x_j for row i (MatVec(1, x, 0, y), matrix_square_sparse.cpp:218-242)
@@ -225,6 +243,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_pcg(Arena A, const int* list,
   const DevParams& P = A.prm[inst];
   const double tol = tol_in >= 0 ? tol_in : P.tol;
   const int maxit = maxit_in >= 0 ? maxit_in : P.maxit;
+  const bool serial = (P.flags & 1) != 0;
   const int v0 = A.voff[inst], v1 = A.voff[inst + 1];
   const int d0 = 3 * v0, d1 = 3 * v1;
   double *x = A.dx, *r = A.r, *p = A.p, *z = A.z;
@@ -233,7 +252,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_pcg(Arena A, const int* list,
     r[i] = A.b[i];
   }
   __syncthreads();
-  const double s0 = cta_dot(r, r, d0, d1, sh);
+  const double s0 = cta_dot(r, r, d0, d1, sh, serial);
   if (s0 < 1.0e-30) {
     if (threadIdx.x == 0) {
       A.st[inst].solver_conv = 0.0;
@@ -247,18 +266,18 @@ __global__ void __launch_bounds__(kSolveThreads) k_pcg(Arena A, const int* list,
   ilu_apply(A, inst, z);
   for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) p[i] = z[i];
   __syncthreads();
-  double rPr = cta_dot(r, z, d0, d1, sh);
+  double rPr = cta_dot(r, z, d0, d1, sh, serial);
   for (int it = 0; it < maxit; it++) {
     for (int i = v0 + threadIdx.x; i < v1; i += blockDim.x) spmv_row(A, i, p, z);  // Ap in z
     __syncthreads();
-    const double pAp = cta_dot(p, z, d0, d1, sh);
+    const double pAp = cta_dot(p, z, d0, d1, sh, serial);
     const double alpha = rPr / pAp;
     for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) {
       r[i] += -alpha * z[i];
       x[i] += +alpha * p[i];
     }
     __syncthreads();
-    const double sq = cta_dot(r, r, d0, d1, sh);
+    const double sq = cta_dot(r, r, d0, d1, sh, serial);
     if (sq * inv0 < tol * tol) {
       if (threadIdx.x == 0) {
         A.st[inst].solver_conv = sqrt(sq * inv0);
@@ -269,13 +288,13 @@ __global__ void __launch_bounds__(kSolveThreads) k_pcg(Arena A, const int* list,
     for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) z[i] = r[i];
     __syncthreads();
     ilu_apply(A, inst, z);
-    const double rPr1 = cta_dot(r, z, d0, d1, sh);
+    const double rPr1 = cta_dot(r, z, d0, d1, sh, serial);
     const double beta = rPr1 / rPr;
     rPr = rPr1;
     for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) p[i] = z[i] + beta * p[i];
     __syncthreads();
   }
-  const double sq = cta_dot(r, r, d0, d1, sh);
+  const double sq = cta_dot(r, r, d0, d1, sh, serial);
   if (threadIdx.x == 0) {
     A.st[inst].solver_conv = sqrt(sq * inv0);
     A.st[inst].solver_iterations = maxit;
@@ -320,7 +339,8 @@ __global__ void k_cg_start(Arena A, double tol_in, int maxit_in) {
   const DevParams& P = A.prm[inst];
   const double tol = tol_in >= 0 ? tol_in : P.tol;
   const int maxit = maxit_in >= 0 ? maxit_in : P.maxit;
-  const double s0 = chunk_total(A.part, A.chunk_lo[inst], A.chunk_hi[inst]);
+  const double s0 = (P.flags & 1) ? serial_dot(A.b, A.b, 3 * A.voff[inst], 3 * A.voff[inst + 1])
+                                   : chunk_total(A.part, A.chunk_lo[inst], A.chunk_hi[inst]);
   InstState& S = A.st[inst];
   S.sq[1] = s0;  // iteration 1 reads parity 1
   S.solver_iterations = maxit;
@@ -358,7 +378,7 @@ __global__ void __launch_bounds__(kChunk) k_cg_update(Arena A, int it) {
   const int c = blockIdx.x;
   const int inst = A.chunk_inst[c];
   if (!A.active[inst] || A.st[inst].done) return;
-  const double pAp = chunk_total(A.part, A.chunk_lo[inst], A.chunk_hi[inst]);
+  const double pAp = (A.prm[inst].flags & 1) ? A.st[inst].dot[0] : chunk_total(A.part, A.chunk_lo[inst], A.chunk_hi[inst]);
   const double alpha = A.st[inst].sq[it & 1] / pAp;
   const int row = A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk + threadIdx.x;
   double s = 0.0;
@@ -385,7 +405,7 @@ __global__ void __launch_bounds__(kChunk) k_cg_direction(Arena A, int it, double
   const double tol = tol_in >= 0 ? tol_in : P.tol;
   InstState& S = A.st[inst];
   const double sq = S.sq[it & 1];
-  const double sqn = chunk_total(A.part + A.nchunk, A.chunk_lo[inst], A.chunk_hi[inst]);
+  const double sqn = (P.flags & 1) ? S.dot[1] : chunk_total(A.part + A.nchunk, A.chunk_lo[inst], A.chunk_hi[inst]);
   const bool first = (c == A.chunk_lo[inst]);
   if (sqn * S.inv0 < tol * tol) {
     if (first && threadIdx.x == 0) {
@@ -410,6 +430,18 @@ __global__ void __launch_bounds__(kChunk) k_cg_direction(Arena A, int it, double
   }
 }
 
+// serial inner products of the cloths that ask for them (one thread per cloth):
+// which = 0: p.Ap into dot[0]; which = 1: r.r into dot[1]
+__global__ void k_cg_serial_dot(Arena A, int which) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= A.ni || !A.active[inst] || A.st[inst].done || !(A.prm[inst].flags & 1)) return;
+  const int lo = 3 * A.voff[inst], hi = 3 * A.voff[inst + 1];
+  if (which == 0)
+    A.st[inst].dot[0] = serial_dot(A.p, A.z, lo, hi);
+  else
+    A.st[inst].dot[1] = serial_dot(A.r, A.r, lo, hi);
+}
+
 __global__ void k_spmv_all(Arena A, const double* x, double* y) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.nv) return;
@@ -420,13 +452,17 @@ __global__ void k_spmv_all(Arena A, const double* x, double* y) {
 
 void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s) {
   if (n <= 0) return;
+  prof_begin(PK_ILU_FACTOR, s);
   k_ilu_factor<<<n, kSolveThreads, 0, s>>>(A, list);
+  prof_end(PK_ILU_FACTOR, s);
   g_launches++;
 }
 
 void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s) {
   if (n <= 0) return;
+  prof_begin(PK_PCG, s);
   k_pcg<<<n, kSolveThreads, 0, s>>>(A, list, tol, maxit);
+  prof_end(PK_PCG, s);
   g_launches++;
 }
 
@@ -436,10 +472,24 @@ void launch_cg_init(const Arena& A, double tol, int maxit, cudaStream_t s) {
   g_launches += 2;
 }
 
-void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, cudaStream_t s) {
+void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, bool serial, cudaStream_t s) {
+  prof_begin(PK_CG_SPMV, s);
   k_cg_spmv<<<A.nchunk, kChunk, 0, s>>>(A);
+  prof_end(PK_CG_SPMV, s);
+  if (serial) {
+    k_cg_serial_dot<<<(A.ni + 127) / 128, 128, 0, s>>>(A, 0);
+    g_launches++;
+  }
+  prof_begin(PK_CG_UPDATE, s);
   k_cg_update<<<A.nchunk, kChunk, 0, s>>>(A, it);
+  prof_end(PK_CG_UPDATE, s);
+  if (serial) {
+    k_cg_serial_dot<<<(A.ni + 127) / 128, 128, 0, s>>>(A, 1);
+    g_launches++;
+  }
+  prof_begin(PK_CG_DIRECTION, s);
   k_cg_direction<<<A.nchunk, kChunk, 0, s>>>(A, it, tol, maxit);
+  prof_end(PK_CG_DIRECTION, s);
   g_launches += 3;
 }
 

@@ -2,6 +2,7 @@
 // for assembly, solvers and collision).
 #pragma once
 #include "arena.h"
+#include "prof.h"
 
 namespace cs {
 
@@ -32,7 +33,7 @@ void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s);
 void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s);
 // CG building blocks on all cloths with A.active set
 void launch_cg_init(const Arena& A, double tol, int maxit, cudaStream_t s);
-void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, cudaStream_t s);
+void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, bool serial, cudaStream_t s);
 void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s);
 
 // --- collision (k_collide.cu) ------------------------------------------------

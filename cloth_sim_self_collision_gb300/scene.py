@@ -66,6 +66,7 @@ class Params:
     obstacle_kind: int = OBSTACLE_SPHERE_SOLID
     solver_kind: int = SOLVER_ILU_PCG
     maxit: int = 100
+    flags: int = 0  # CS_FLAG_EXACT_DOTS = 1: serial inner products (bit-exact FP64 path)
 
 
 @dataclasses.dataclass

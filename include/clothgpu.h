@@ -46,6 +46,12 @@ extern "C" {
 #define CS_SOLVER_ILU_PCG 0   /* Solve_PCG with block ILU(0), ilu_sparse.cpp:628     */
 #define CS_SOLVER_CG 1        /* Solve_CG, matrix_square_sparse.cpp:338              */
 
+/* cs_params.flags */
+#define CS_FLAG_EXACT_DOTS 1  /* Krylov inner products as one running sum in dof order, like the
+                                 reference's InnerProduct (matrix_square_sparse.cpp:313): the FP64
+                                 path then reproduces the reference bit for bit, at the cost of a
+                                 serial sum per inner product.  Off: deterministic tree sums. */
+
 /* Parameters of one cloth: the arguments of StepTime_InternalDynamicsILU
  * (solve_internal_sparse.h:255-275) and GetIntermidiateVelocityContactResolved
  * (self_collision_cloth.h:21-34), plus the solver tolerance and cap that the
@@ -65,7 +71,7 @@ typedef struct {
   int obstacle_kind;
   int solver_kind;
   int maxit;
-  int reserved;
+  int flags; /* CS_FLAG_* */
 } cs_params;
 
 /* Per-frame counters of one cloth (the reference prints these,
@@ -102,6 +108,8 @@ void cs_destroy(cs_ctx *ctx);
 const char *cs_last_error(const cs_ctx *ctx);
 int cs_set_precision(cs_ctx *ctx, int precision);
 int cs_synchronize(cs_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for recording events around calls. */
+void *cs_stream(const cs_ctx *ctx);
 
 /* ---- cloths ---------------------------------------------------------------- */
 /* Adds a cloth: builds its topology on the host (matrix pattern as in
@@ -189,9 +197,25 @@ int cs_element_bend(cs_ctx *ctx, int n, const double *C, const double *c, double
 int cs_element_contact(cs_ctx *ctx, int n, const double *c, const cs_params *prm, double *W, double *dW,
                        double *ddW);
 
+/* ---- whole-arena state I/O ------------------------------------------------------ */
+/* States of every cloth in the order they were added (x and v of 3 doubles per
+ * vertex each, cloths back to back): one copy each way for the whole arena.  Either
+ * pointer may be null. */
+int cs_set_states(cs_ctx *ctx, const double *x, const double *v);
+int cs_get_states(cs_ctx *ctx, double *x, double *v);
+/* Total vertices of the context (length of the state arrays / 3). */
+long long cs_num_vertices(const cs_ctx *ctx);
+
 /* ---- counters ------------------------------------------------------------------ */
 /* Kernel launches issued by this context since creation (for launch accounting). */
 long long cs_launch_count(const cs_ctx *ctx);
+/* Device timing of kernel classes with CUDA events recorded on the context's
+ * stream around each launch: enable (1) / disable (0) and clear the totals; read
+ * the total milliseconds and launch count of one class ("cg_spmv", "traverse",
+ * "narrow", "refit", "tri_elements", "slot_reduce", "rhs", "ilu_factor", "pcg",
+ * "cg_update", "cg_direction", "impulse"). */
+int cs_profile(cs_ctx *ctx, int enable);
+int cs_profile_read(cs_ctx *ctx, const char *kernel, double *total_ms, long long *launches);
 
 #ifdef __cplusplus
 }

@@ -53,7 +53,7 @@ typedef struct {
   int obstacle_kind;
   int solver_kind;
   int maxit;
-  int reserved;
+  int flags; /* ignored: the oracle always sums inner products serially, like the reference */
 } co_params;
 
 /* Per-frame counters, filled by co_step / co_resolve. */

@@ -32,7 +32,7 @@ class CoParams(ctypes.Structure):
         ("contact_clearance", ctypes.c_double), ("obs_center", ctypes.c_double * 3),
         ("obs_radius", ctypes.c_double), ("tol", ctypes.c_double),
         ("obstacle_kind", ctypes.c_int), ("solver_kind", ctypes.c_int),
-        ("maxit", ctypes.c_int), ("reserved", ctypes.c_int),
+        ("maxit", ctypes.c_int), ("flags", ctypes.c_int),
     ]
 
     @classmethod
