@@ -255,7 +255,7 @@ def native(args):
         "config": workload_config(len(cloths), nv, "fp64 (plain path; one arena, one launch sequence per frame)"),
         "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
         "e2e": e2e, "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
-        "kernel_ms": {k: round(v[0], 3) for k, v in prof.items()},
+        "kernel_ms": {k: [round(v[0], 3), v[1]] for k, v in prof.items()},
     }
     if not args.no_cpu:
         line["cpu_baseline"] = run_cpu_baseline(cloths)

@@ -163,63 +163,52 @@ __device__ __forceinline__ void emit(const ContactBufs& C, int fv, int j0, int j
 __constant__ int kEE[9][4] = {{0, 1, 0, 1}, {0, 1, 1, 2}, {0, 1, 2, 0}, {1, 2, 0, 1}, {1, 2, 1, 2},
                               {1, 2, 2, 0}, {2, 0, 0, 1}, {2, 0, 1, 2}, {2, 0, 2, 0}};
 
-// narrow phase of one leaf pair (bvh_aabb.cpp:473-536 proximity, 836-901 CCD)
+// Narrow phase (bvh_aabb.cpp:473-536 proximity, 836-901 CCD): one thread per
+// (elementary test, leaf pair), test-major, so that a warp runs one kind of
+// test (the FP64 paths of the 15 tests differ widely).  Tests 0-2: face a vs
+// the vertices of b; 3-5: face b vs the vertices of a; 6-14: the 9 edge pairs.
 __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs, double delta_override,
                          int npairs) {
-  const int pid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pid >= npairs) return;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= 15LL * npairs) return;
+  const int test = (int)(tid / npairs);
+  const int pid = (int)(tid - (long long)test * npairs);
   const int2 pr = C.pairs[pid];
   const int na = pr.x, nb = pr.y;
   const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
   const int inst = A.tinst[ta];
   const DevParams& P = A.prm[inst];
   const double delta = delta_override >= 0 ? delta_override : P.contact_clearance;
-  int ia[3], ib[3];
-  V3<double> p[3], q[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    ia[k] = A.tri[3 * ta + k];
-    ib[k] = A.tri[3 * tb + k];
-    p[k] = ld3(xs, ia[k]);
-    q[k] = ld3(xs, ib[k]);
+  if (test < 6) {
+    const bool fa = test < 3;
+    const int tf = fa ? ta : tb, tv = fa ? tb : ta, k = fa ? test : test - 3;
+    const int f0 = A.tri[3 * tf], f1 = A.tri[3 * tf + 1], f2 = A.tri[3 * tf + 2], q = A.tri[3 * tv + k];
+    if (q == f0 || q == f1 || q == f2) return;
+    const V3<double> p0 = ld3(xs, f0), p1 = ld3(xs, f1), p2 = ld3(xs, f2), p3 = ld3(xs, q);
+    if (!ccd) {
+      // the reference passes aBB[triangle index]: the box of the node whose
+      // index equals the triangle's index within its cloth
+      const Box bb = A.box[A.noff[inst] + (tf - A.toff[inst])];
+      if (fv_proximity(f0, f1, f2, q, p0, p1, p2, p3, bb, delta)) emit(C, 1, f0, f1, f2, q, na, nb, test);
+    } else {
+      const Box bb = A.box[fa ? na : nb];
+      if (fv_ccd(f0, f1, f2, q, p0, p1, p2, p3, end_pos(xs, vs, f0, P.dt), end_pos(xs, vs, f1, P.dt),
+                 end_pos(xs, vs, f2, P.dt), end_pos(xs, vs, q, P.dt), bb))
+        emit(C, 1, f0, f1, f2, q, na, nb, test);
+    }
+    return;
   }
+  const int k = test - 6;
+  const int i0 = A.tri[3 * ta + kEE[k][0]], i1 = A.tri[3 * ta + kEE[k][1]];
+  const int j0 = A.tri[3 * tb + kEE[k][2]], j1 = A.tri[3 * tb + kEE[k][3]];
+  if (i0 == j0 || i0 == j1 || i1 == j0 || i1 == j1) return;
+  const V3<double> p0 = ld3(xs, i0), p1 = ld3(xs, i1), q0 = ld3(xs, j0), q1 = ld3(xs, j1);
   if (!ccd) {
-    // the reference passes aBB[triangle index]: the box of the node whose
-    // index equals the triangle's index within its cloth
-    const Box bba = A.box[A.noff[inst] + (ta - A.toff[inst])];
-    const Box bbb = A.box[A.noff[inst] + (tb - A.toff[inst])];
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-      if (fv_proximity(ia[0], ia[1], ia[2], ib[k], p[0], p[1], p[2], q[k], bba, delta))
-        emit(C, 1, ia[0], ia[1], ia[2], ib[k], na, nb, k);
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-      if (fv_proximity(ib[0], ib[1], ib[2], ia[k], q[0], q[1], q[2], p[k], bbb, delta))
-        emit(C, 1, ib[0], ib[1], ib[2], ia[k], na, nb, 3 + k);
-    for (int k = 0; k < 9; k++) {
-      const int e0 = kEE[k][0], e1 = kEE[k][1], f0 = kEE[k][2], f1 = kEE[k][3];
-      if (ee_proximity(ia[e0], ia[e1], ib[f0], ib[f1], p[e0], p[e1], q[f0], q[f1], delta))
-        emit(C, 0, ia[e0], ia[e1], ib[f0], ib[f1], na, nb, 6 + k);
-    }
+    if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
   } else {
-    V3<double> pe[3], qe[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      pe[k] = end_pos(xs, vs, ia[k], P.dt);
-      qe[k] = end_pos(xs, vs, ib[k], P.dt);
-    }
-    const Box bba = A.box[na], bbb = A.box[nb];
-    for (int k = 0; k < 3; k++)
-      if (fv_ccd(ia[0], ia[1], ia[2], ib[k], p[0], p[1], p[2], q[k], pe[0], pe[1], pe[2], qe[k], bba))
-        emit(C, 1, ia[0], ia[1], ia[2], ib[k], na, nb, k);
-    for (int k = 0; k < 3; k++)
-      if (fv_ccd(ib[0], ib[1], ib[2], ia[k], q[0], q[1], q[2], p[k], qe[0], qe[1], qe[2], pe[k], bbb))
-        emit(C, 1, ib[0], ib[1], ib[2], ia[k], na, nb, 3 + k);
-    for (int k = 0; k < 9; k++) {
-      const int e0 = kEE[k][0], e1 = kEE[k][1], f0 = kEE[k][2], f1 = kEE[k][3];
-      if (ee_ccd(ia[e0], ia[e1], ib[f0], ib[f1], p[e0], p[e1], q[f0], q[f1], pe[e0], pe[e1], qe[f0], qe[f1]))
-        emit(C, 0, ia[e0], ia[e1], ib[f0], ib[f1], na, nb, 6 + k);
-    }
+    if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, end_pos(xs, vs, i0, P.dt), end_pos(xs, vs, i1, P.dt),
+               end_pos(xs, vs, j0, P.dt), end_pos(xs, vs, j1, P.dt)))
+      emit(C, 0, i0, i1, j0, j1, na, nb, test);
   }
 }
 
@@ -675,7 +664,7 @@ void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* 
                    double delta_override, int npairs, cudaStream_t s) {
   if (npairs <= 0) return;
   prof_begin(PK_NARROW, s);
-  k_narrow<<<nblk(npairs), kT, 0, s>>>(A, C, ccd, xs, vs, delta_override, npairs);
+  k_narrow<<<nblk(15LL * npairs), kT, 0, s>>>(A, C, ccd, xs, vs, delta_override, npairs);
   prof_end(PK_NARROW, s);
   g_launches++;
 }

@@ -2,10 +2,13 @@
 
 Tolerances: every stage whose arithmetic is a fixed sequence of IEEE double
 operations is compared bit for bit (element kernels, assembly, ILU factor,
-refits, contact sets, impulses, impact zones, velocity update).  The Krylov
-solves sum inner products as a tree instead of one running sum, so their
-results (and anything downstream of them) are compared with
-    max |gpu - oracle| <= RTOL * max(1, max |oracle|),   RTOL = 1e-9.
+refits, contact sets, impulses, impact zones, velocity update), and so are whole
+frames and trajectories with serial inner products (CS_FLAG_EXACT_DOTS).  In
+the default mode the Krylov solves sum inner products as a tree instead of one
+running sum; their results are compared with
+    max |gpu - oracle| <= RTOL * max(1, max |oracle|),   RTOL = 1e-9
+for a single solve, and along trajectories by the solver's own criterion
+(relative residual below the tolerance on the oracle's assembled system).
 """
 import json
 import os
@@ -211,26 +214,46 @@ def test_trajectory_bit_exact(ctx, name, frames):
     ctx.remove_cloth(cid)
 
 
+def residual_ratio(vd, vc, rp, ci, b, x):
+    """||b - A x|| / ||b|| for the 3x3 block matrix (diagonal blocks vd, off-diagonal vc)."""
+    X = x.reshape(-1, 3)
+    y = np.einsum("nij,nj->ni", vd.reshape(-1, 3, 3), X)
+    vcb = vc.reshape(-1, 3, 3)
+    rows = np.repeat(np.arange(rp.size - 1), np.diff(rp))
+    np.add.at(y, rows, np.einsum("sij,sj->si", vcb, X[ci]))
+    return np.linalg.norm(b - y.reshape(-1)) / np.linalg.norm(b)
+
+
 @pytest.mark.parametrize("name", ["small_21", "fold_31"])
 def test_fast_mode_implicit_frames(ctx, oracle_port, name):
-    """Tree-summed inner products: the implicit step stays within RTOL of the
-    oracle along the oracle's trajectory."""
+    """Tree-summed inner products: along the oracle's trajectory, the GPU's
+    implicit-step increment meets the solver's own criterion on the oracle's
+    assembled system (relative residual below the tolerance), with the
+    iteration count within one of the oracle's."""
     c = scene_for(name)
     cid = ctx.add_cloth(c)
     orc = O.OracleCloth(oracle_port, c)
+    rp, ci = orc.pattern()
     for f in range(0, 100, 5):
+        x0 = orc.x.copy()
+        vd, vc, b = orc.assemble(orc.x, orc.v)
         xa, va, sa = ctx.implicit(cid, orc.x, orc.v)
         xb, vb, sb = orc.implicit(orc.x, orc.v)
-        assert close(xa, xb), (name, f)
-        assert abs(sa["solver_iterations"] - sb["solver_iterations"]) <= 1
+        assert abs(sa["solver_iterations"] - sb["solver_iterations"]) <= 1, (name, f)
+        ra = residual_ratio(vd, vc, rp, ci, b, xa - x0)
+        rb = residual_ratio(vd, vc, rp, ci, b, xb - x0)
+        assert ra <= 1.5 * max(c.params.tol, rb), (name, f, ra, rb)
         orc.step(5)
     ctx.remove_cloth(cid)
 
 
-def test_fast_mode_trajectory_first_divergence(ctx, oracle_port):
-    """Tree-summed inner products over 300 frames of the 21x21 sheet: positions
-    stay within 1e-6 relative of the oracle (contact thresholds make longer
-    trajectories chaotic; the first frame beyond RTOL is reported)."""
+def test_fast_mode_trajectory(ctx, oracle_port):
+    """Tree-summed inner products over 300 frames of the 21x21 sheet: within RTOL
+    of the oracle until the first self-contact frame; afterwards contact
+    thresholds make the trajectory chaotic, so only the first frame beyond RTOL
+    is reported."""
+    meta, _ = load("small_21")
+    first_contact = next(f for f, s in enumerate(meta["steps"]) if s["stats"]["n_prx"] or s["stats"]["n_ccd"][0])
     c = scene.config_small()
     cid = ctx.add_cloth(c)
     orc = O.OracleCloth(oracle_port, c)
@@ -239,11 +262,13 @@ def test_fast_mode_trajectory_first_divergence(ctx, oracle_port):
         orc.step(1)
         ctx.step(1)
         xa, _ = ctx.get_state(cid)
+        assert np.all(np.isfinite(xa))
         err = np.abs(xa - orc.x).max() / max(1.0, np.abs(orc.x).max())
+        if f < first_contact:
+            assert err <= RTOL, (f, err)
         if first is None and err > RTOL:
             first = f
-        assert err <= 1e-6, (f, err, first)
-    print("first frame beyond 1e-9:", first)
+    print(f"first self-contact frame {first_contact}, first frame beyond RTOL: {first}")
     ctx.remove_cloth(cid)
 
 
