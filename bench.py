@@ -198,6 +198,7 @@ def native(args):
     for name in ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit",
                  "traverse", "narrow", "impulse", "pcg", "ilu_factor"):
         prof[name] = ctx.profile_read(name)
+    counts = {k: ctx.profile_read(k)[1] for k in ("pairs", "candidates", "contacts", "detections")}
     ctx.profile(False)
     if world > 1:
         import torch.distributed as dist
@@ -256,6 +257,7 @@ def native(args):
         "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
         "e2e": e2e, "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
         "kernel_ms": {k: [round(v[0], 3), v[1]] for k, v in prof.items()},
+        "contact_counts": counts,
     }
     if not args.no_cpu:
         line["cpu_baseline"] = run_cpu_baseline(cloths)

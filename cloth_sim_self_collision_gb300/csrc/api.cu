@@ -483,6 +483,10 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
   int total = 0;
   CK(cudaMemcpyAsync(&total, c->C.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
   pull_states(c);
+  prof_count("pairs", npairs);
+  prof_count("candidates", ncand);
+  prof_count("contacts", total);
+  prof_count("detections", 1);
   return total;
 }
 

@@ -21,6 +21,8 @@ std::vector<cudaEvent_t> g_free;
 cudaEvent_t g_open[PK_COUNT];
 double g_ms[PK_COUNT];
 long long g_n[PK_COUNT];
+const char* const kCountNames[4] = {"pairs", "candidates", "contacts", "detections"};
+long long g_counts[4];
 
 cudaEvent_t get_event() {
   if (!g_free.empty()) {
@@ -68,10 +70,23 @@ void prof_reset() {
   prof_collect();
   std::memset(g_ms, 0, sizeof(g_ms));
   std::memset(g_n, 0, sizeof(g_n));
+  std::memset(g_counts, 0, sizeof(g_counts));
+}
+
+void prof_count(const char* name, long long n) {
+  if (!g_on) return;
+  for (int k = 0; k < 4; k++)
+    if (std::strcmp(name, kCountNames[k]) == 0) g_counts[k] += n;
 }
 
 bool prof_read(const char* name, double* total_ms, long long* launches) {
   prof_collect();
+  for (int k = 0; k < 4; k++)
+    if (std::strcmp(name, kCountNames[k]) == 0) {
+      if (total_ms) *total_ms = 0;
+      if (launches) *launches = g_counts[k];
+      return true;
+    }
   for (int k = 0; k < PK_COUNT; k++)
     if (std::strcmp(name, kProfNames[k]) == 0) {
       if (total_ms) *total_ms = g_ms[k];

@@ -31,5 +31,7 @@ void prof_enable(bool on);
 void prof_collect();
 void prof_reset();
 bool prof_read(const char* name, double* total_ms, long long* launches);
+// host-side counters read through prof_read: "pairs", "candidates", "contacts", "detections"
+void prof_count(const char* name, long long n);
 
 }  // namespace cs
