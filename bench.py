@@ -138,6 +138,63 @@ def run_cpu_baseline(cloths, budget_s: float = 12.0) -> dict:
 
 
 # --------------------------------------------------------------------------------------
+def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
+    """K resident frames of every cloth in the context; per-frame CUDA events on
+    the library's stream.  Returns (per-frame ms list, profile dict, launches)."""
+    import torch
+
+    ctx.step(warmup)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count()
+    ctx.profile(True)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for k in range(steps):
+        ctx.step(1)
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    prof = {name: ctx.profile_read(name) for name in profile_names}
+    counts = {k: ctx.profile_read(k)[1] for k in ("pairs", "candidates", "contacts", "detections")}
+    ctx.profile(False)
+    return step_ms, prof, counts, ctx.launch_count() - launches0
+
+
+PROFILED = ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit", "traverse",
+            "narrow", "impulse", "pcg", "ilu_factor", "mx_spmv", "mx_update", "mx_direction", "mx_residual")
+
+
+def plain_one_per_launch(cloths, device, frames: int, budget_s: float = 8.0) -> dict:
+    """The plain FP64 path, one cloth per arena and launch sequence, on a sample."""
+    import torch
+
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    ctx = ClothContext(device, "fp64")
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+    vs, ms, used = 0, 0.0, 0
+    for c in cloths:
+        cid = ctx.add_cloth(c)
+        ctx.step(1)  # builds the arena, first frame untimed
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.step(frames)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+        vs += c.np * frames
+        used += 1
+        ctx.remove_cloth(cid)
+        if ms / 1e3 > budget_s:
+            break
+    ctx.close()
+    return {"value": vs / (ms / 1e3), "unit": UNIT,
+            "sample": f"first {used} cloths of the workload, each alone in its own arena (FP64, tree-summed "
+                      f"inner products), frames 2..{frames + 1}"}
+
+
 def native(args):
     import torch
 
@@ -154,60 +211,61 @@ def native(args):
     B.build()
     torch.cuda.set_device(local)
     cloths = scene.config_batch(count=args.cloths)
-    ctx = ClothContext(local, "fp64")
-    ids = [ctx.add_cloth(c) for c in cloths]
-    nv = ctx.num_vertices()
-    nb_total = 0
-    for i in ids:
-        rp, _ = ctx.pattern(i)
-        nb_total += int(rp[-1])
-    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    # warm-up (also builds and uploads the arena)
-    ctx.step(args.warmup)
-    ctx.synchronize()
-    torch.cuda.synchronize()
+    results = {}
+    for prec in (["mixed", "fp64"] if args.precision == "both" else [args.precision]):
+        ctx = ClothContext(local, prec)
+        ids = [ctx.add_cloth(c) for c in cloths]
+        nv = ctx.num_vertices()
+        nb_total = sum(int(ctx.pattern(i)[0][-1]) for i in ids)
+        stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+        clocks = ClockSampler(local)
+        barrier()
+        clocks.start()
+        step_ms, prof, counts, launches = timed_batch(ctx, ids, args.steps, args.warmup, stream, nv, PROFILED)
+        clk = clocks.stop()
+        barrier()
+        total_ms = sum(step_ms)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([total_ms], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+        res = {"value": world * nv * args.steps / (total_ms / 1e3), "ms_per_step": total_ms / args.steps,
+               "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+               "prof": prof, "counts": counts, "launches": launches, "clocks": clk, "nv": nv, "nb": nb_total}
+        if prec == results.get("headline", prec) or not results:
+            # end to end through the C ABI: pinned host state in, frame, state out
+            xs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
+            vs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
+            ctx.get_states(xs.numpy(), vs.numpy())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(args.steps):
+                ctx.set_states(xs.numpy(), vs.numpy())
+                ctx.step(1)
+                ctx.get_states(xs.numpy(), vs.numpy())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            e2e_ms = e0.elapsed_time(e1)
+            res["e2e"] = {"value": world * nv * args.steps / (e2e_ms / 1e3), "unit": UNIT,
+                          "h2d_bytes_per_step": 2 * 3 * nv * 8, "d2h_bytes_per_step": 2 * 3 * nv * 8}
+            results["headline"] = prec
+        results[prec] = res
+        ctx.close()
+    head = results[results["headline"]]
+    plain = None
+    if not args.no_plain:
+        plain = plain_one_per_launch(cloths, local, frames=3)
 
-    # timed region: K frames, resident state, per-frame events on the library's stream
-    launches0 = ctx.launch_count()
-    ctx.profile(True)
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier()
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    ev[0].record(stream)
-    iters = []
-    for k in range(args.steps):
-        ctx.step(1)
-        ev[k + 1].record(stream)
-        iters.append(sum(ctx.stats(i)["solver_iterations"] for i in ids[:1]))
-    torch.cuda.synchronize()
-    ctx.synchronize()
-    barrier()
-    clk = clocks.stop()
-    launches = ctx.launch_count() - launches0
-    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_ms = sum(step_ms)
-    prof = {}
-    for name in ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit",
-                 "traverse", "narrow", "impulse", "pcg", "ilu_factor"):
-        prof[name] = ctx.profile_read(name)
-    counts = {k: ctx.profile_read(k)[1] for k in ("pairs", "candidates", "contacts", "detections")}
-    ctx.profile(False)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * nv * args.steps / (total_ms / 1e3)
-
-    # roofline of the dominant kernel class
+    # roofline of the dominant kernel class of the headline run
+    prof = head["prof"]
     top = max(prof, key=lambda k: prof[k][0])
     peaks = read_peaks()
     roof = {"kernel": top, "bound": "hbm", "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -215,50 +273,43 @@ def native(args):
     ms, n = prof[top]
     roof["launches"] = n
     roof["avg_launch_us"] = 1e3 * ms / max(n, 1)
-    if top == "cg_spmv":
-        # every launch covers the rows of the cloths whose CG has not converged;
-        # bound from above by the whole arena per launch
-        per_launch = spmv_bytes(nv, nb_total)
-        roof["achieved"] = per_launch / (ms / max(n, 1) / 1e3) / 1e9
+    per_launch = None
+    if top == "cg_spmv" or top == "mx_residual":
+        per_launch = spmv_bytes(head["nv"], head["nb"], 8)
+    elif top == "mx_spmv":
+        per_launch = spmv_bytes(head["nv"], head["nb"], 4)
+    if per_launch is not None:
         roof["bytes_per_launch"] = per_launch
-        roof["bytes_note"] = "whole-arena SpMV bytes; launches late in the solve skip converged cloths"
-    else:
-        roof["achieved"] = None
-    if roof["achieved"] is not None:
+        roof["bytes_note"] = "whole-arena SpMV bytes per launch; later launches skip converged cloths"
+        roof["achieved"] = per_launch / (ms / max(n, 1) / 1e3) / 1e9
         roof["frac"] = roof["achieved"] / roof["peak"]
     else:
+        roof["achieved"] = None
         roof["frac"] = None
-
-    # end to end through the C ABI: pinned host state in, frame, state out
-    xs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
-    vs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
-    ctx.get_states(xs.numpy(), vs.numpy())
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        ctx.set_states(xs.numpy(), vs.numpy())
-        ctx.step(1)
-        ctx.get_states(xs.numpy(), vs.numpy())
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    e2e = {"value": world * nv * args.steps / (e2e_ms / 1e3), "unit": UNIT,
-           "h2d_bytes_per_step": 2 * 3 * nv * 8, "d2h_bytes_per_step": 2 * 3 * nv * 8}
 
     if rank != 0:
         return
+    hp = results["headline"]
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(len(cloths), nv, "fp64 (plain path; one arena, one launch sequence per frame)"),
-        "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
-        "e2e": e2e, "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
-        "kernel_ms": {k: [round(v[0], 3), v[1]] for k, v in prof.items()},
-        "contact_counts": counts,
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if hp == "mixed" else "f64", "data": "synthetic",
+        "config": workload_config(len(cloths), head["nv"], hp),
+        "p50_step_ms": head["p50_step_ms"], "p99_step_ms": head["p99_step_ms"],
+        "e2e": head["e2e"], "roofline": roof, "gpu_launches": int(head["launches"]), "clocks": head["clocks"],
+        "kernel_ms": {k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]},
+        "contact_counts": head["counts"],
     }
+    for prec in ("mixed", "fp64"):
+        if prec in results and prec != hp:
+            r = results[prec]
+            line[f"batched_{prec}"] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
+                                       "p50_step_ms": r["p50_step_ms"], "p99_step_ms": r["p99_step_ms"],
+                                       "kernel_ms": {k: [round(v[0], 3), v[1]] for k, v in r["prof"].items() if v[1]}}
+    if plain is not None:
+        line["plain_gpu_fp64_one_per_launch"] = plain
+        line["vs_plain_gpu"] = head["value"] / plain["value"]
     if not args.no_cpu:
         line["cpu_baseline"] = run_cpu_baseline(cloths)
     print(json.dumps(line), flush=True)
@@ -347,6 +398,9 @@ def main():
     ap.add_argument("--cloths", type=int, default=512)
     ap.add_argument("--ref-cloths", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-cloth-per-launch FP64 sample")
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
+                    help="both: mixed is the headline, FP64 batched reported beside it")
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
         raise SystemExit("need --steps >= 1 and --warmup >= 0")

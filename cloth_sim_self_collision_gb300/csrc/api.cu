@@ -351,6 +351,62 @@ void rebuild(cs_ctx* c) {
   A.inzone = m.alloc<int>(NV);
   CK(cudaMemsetAsync(A.inzone, 0, sizeof(int) * (size_t)std::max(NV, 1), s));
   c->d_list = m.alloc<int>(std::max(ni, 1));
+  // mixed precision: SELL-32 slices of every cloth's rows (32 rows per slice,
+  // padded to the widest row with zero blocks pointing at the slice's own row)
+  {
+    std::vector<int> slice_inst, slice_row0, slice_w, slice_lo(ni), slice_hi(ni), col32;
+    std::vector<long long> slice_voff, slice_coff, sell_pos((size_t)NB + NV);
+    long long vtot = 0, ctot = 0;
+    for (int i = 0; i < ni; i++) {
+      const ClothTopo& t = c->cloths[c->order[i]]->topo;
+      const int vo = c->voff[i], bo = c->boff[i];
+      slice_lo[i] = (int)slice_inst.size();
+      for (int r0 = 0; r0 < t.np; r0 += 32) {
+        const int n = std::min(32, t.np - r0);
+        int w = 0;
+        for (int l = 0; l < n; l++) w = std::max(w, t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l] + 1);
+        slice_inst.push_back(i);
+        slice_row0.push_back(vo + r0);
+        slice_w.push_back(w);
+        slice_voff.push_back(vtot);
+        slice_coff.push_back(ctot);
+        for (int j = 0; j < w; j++)
+          for (int l = 0; l < 32; l++) {
+            int col = vo + r0;
+            if (l < n) {
+              const int row = r0 + l, len = t.row_ptr[row + 1] - t.row_ptr[row];
+              col = (j < len) ? t.col_idx[t.row_ptr[row] + j] + vo : vo + row;
+              if (j < len) sell_pos[(size_t)bo + t.row_ptr[row] + j] = vtot + 9LL * 32 * j + l;
+              if (j == len) sell_pos[(size_t)NB + vo + row] = vtot + 9LL * 32 * j + l;
+            }
+            col32.push_back(col);
+          }
+        vtot += 9LL * 32 * w;
+        ctot += 32LL * w;
+      }
+      slice_hi[i] = (int)slice_inst.size();
+    }
+    A.nslice = (int)slice_inst.size();
+    A.slice_inst = m.upload(slice_inst, s);
+    A.slice_row0 = m.upload(slice_row0, s);
+    A.slice_w = m.upload(slice_w, s);
+    A.slice_lo = m.upload(slice_lo, s);
+    A.slice_hi = m.upload(slice_hi, s);
+    A.slice_voff = m.upload(slice_voff, s);
+    A.slice_coff = m.upload(slice_coff, s);
+    A.sell_pos = m.upload(sell_pos, s);
+    A.col32 = m.upload(col32, s);
+    A.val32 = m.alloc<float>(vtot);
+    CK(cudaMemsetAsync(A.val32, 0, sizeof(float) * (size_t)std::max(vtot, 1LL), s));
+    A.dinv32 = m.alloc<float>(9 * (size_t)NV);
+    A.r32 = m.alloc<float>(3 * (size_t)NV);
+    A.d32 = m.alloc<float>(3 * (size_t)NV);
+    A.p32 = m.alloc<float>(3 * (size_t)NV);
+    A.q32 = m.alloc<float>(3 * (size_t)NV);
+    A.z32 = m.alloc<float>(3 * (size_t)NV);
+    A.part32 = m.alloc<double>(3 * (size_t)std::max(A.nslice, 1));
+    A.mixed = 1;
+  }
   c->A = A;
   if (ni > 0) launch_quad_factors(A, s);
   alloc_contacts(c, 16 * NT + 4096, 4 * NT + 4096);
@@ -417,9 +473,42 @@ void run_cg(cs_ctx* c, const std::vector<int>& cg, double tol, int maxit) {
   }
 }
 
+// Mixed precision: FP64 refinement cycles around FP32 block-Jacobi CG solves
+// (inner relative residual eta, at most `cap` iterations per cycle).
+void run_mixed(cs_ctx* c, const std::vector<int>& act) {
+  const Arena& A = c->A;
+  const float eta = 1.0e-3f;
+  const int cap = 300, maxcycles = 12;
+  set_active(c, act);
+  launch_mx_outer_init(A, c->stream);
+  for (int cyc = 0; cyc < maxcycles; cyc++) {
+    launch_mx_inner_init(A, c->stream);
+    for (int it = 1; it <= cap; it++) {
+      launch_mx_inner_iteration(A, it, eta, cap, c->stream);
+      if (it % 8 == 0) {
+        pull_states(c);
+        bool all = true;
+        for (int i = 0; i < A.ni; i++)
+          if (act[i] && !c->hst[i].done && !c->hst[i].idone) all = false;
+        if (all) break;
+      }
+    }
+    launch_mx_refine(A, -1.0, maxcycles, c->stream);
+    pull_states(c);
+    bool all = true;
+    for (int i = 0; i < A.ni; i++)
+      if (act[i] && !c->hst[i].done) all = false;
+    if (all) break;
+  }
+}
+
 // solves A dx = b for the active cloths with each cloth's own solver
 void solve(cs_ctx* c, const std::vector<int>& act) {
   const Arena& A = c->A;
+  if (c->precision == CS_PREC_MIXED) {
+    run_mixed(c, act);
+    return;
+  }
   std::vector<int> ilu, cg(A.ni, 0);
   bool any_cg = false;
   for (int i = 0; i < A.ni; i++) {
@@ -804,7 +893,6 @@ int cs_step(cs_ctx* c, int nsteps) {
     if (nsteps < 0) throw ArgError("negative step count");
     ensure(c);
     if (c->A.ni == 0) return;
-    if (c->precision != CS_PREC_FP64) throw ArgError("mixed precision is not available in this build");
     std::vector<int> all(c->A.ni, 1);
     for (int k = 0; k < nsteps; k++) frame(c, all);
     CK(cudaStreamSynchronize(c->stream));

@@ -42,6 +42,13 @@ struct InstState {
   double inv0;
   double rpr;        // PCG: r.Pr
   double dot[2];     // CG with serial inner products: p.Ap, r.r of this iteration
+  // mixed precision: inner FP32 solve state
+  double rz[2];      // r.z of the previous / current inner iteration (by parity)
+  double rr_in0;     // r.r at the start of the inner solve
+  int idone;         // inner solve finished
+  int inner_iters;   // inner iterations of the current inner solve
+  int total_iters;   // inner iterations summed over refinement cycles
+  int cycles;        // refinement cycles
 };
 
 struct Arena {
@@ -77,6 +84,20 @@ struct Arena {
   Box* box = nullptr;
   // impact zones
   int *edge_uv = nullptr, *uf = nullptr, *inzone = nullptr;
+  // mixed precision: FP32 copy of the matrix in warp slices (SELL-32: 32 rows per
+  // slice, blocks of a slice stored entry-major so every load is 32 consecutive
+  // floats), block-Jacobi inverse, FP32 work vectors
+  int nslice = 0;
+  int *slice_inst = nullptr, *slice_row0 = nullptr, *slice_w = nullptr, *slice_lo = nullptr, *slice_hi = nullptr;
+  long long* slice_voff = nullptr;  // float offset of the slice's values
+  long long* slice_coff = nullptr;  // int offset of the slice's column indices
+  long long* sell_pos = nullptr;    // per slot (off-diagonal then diagonal): value offset of entry 0
+  float* val32 = nullptr;
+  int* col32 = nullptr;
+  float* dinv32 = nullptr;          // 9 per vertex
+  float *r32 = nullptr, *d32 = nullptr, *p32 = nullptr, *q32 = nullptr, *z32 = nullptr;
+  double* part32 = nullptr;         // 3 per slice: p.q, r.z, r.r
+  int mixed = 0;                    // mixed-precision arrays present
 };
 
 // scratch for the contact pipeline (grown on demand)

@@ -126,6 +126,11 @@ __global__ void k_slot_reduce(Arena A) {
     const bool fixed = A.bc[row] != 0 || A.bc[col] != 0;
 #pragma unroll
     for (int k = 0; k < 9; k++) A.vcrs[9 * (size_t)s + k] = fixed ? 0.0 : acc[k];
+    if (A.mixed) {
+      float* dst = A.val32 + A.sell_pos[s];
+#pragma unroll
+      for (int k = 0; k < 9; k++) dst[32 * k] = fixed ? 0.f : (float)acc[k];
+    }
     return;
   }
   const int v = s - A.nb;
@@ -144,7 +149,34 @@ __global__ void k_slot_reduce(Arena A) {
   acc[8] += m;
   const bool fixed = A.bc[v] != 0;
 #pragma unroll
-  for (int k = 0; k < 9; k++) A.vdia[9 * (size_t)v + k] = fixed ? ((k % 4 == 0) ? 1.0 : 0.0) : acc[k];
+  for (int k = 0; k < 9; k++) {
+    acc[k] = fixed ? ((k % 4 == 0) ? 1.0 : 0.0) : acc[k];
+    A.vdia[9 * (size_t)v + k] = acc[k];
+  }
+  if (A.mixed) {
+    float* dst = A.val32 + A.sell_pos[s];
+#pragma unroll
+    for (int k = 0; k < 9; k++) dst[32 * k] = (float)acc[k];
+    // block-Jacobi preconditioner: inverse of the diagonal block (identity if singular)
+    const double det = acc[0] * (acc[4] * acc[8] - acc[5] * acc[7]) - acc[1] * (acc[3] * acc[8] - acc[5] * acc[6]) +
+                       acc[2] * (acc[3] * acc[7] - acc[4] * acc[6]);
+    float* D = A.dinv32 + 9 * (size_t)v;
+    if (fabs(det) > 1e-300) {
+      const double r = 1.0 / det;
+      D[0] = (float)(r * (acc[4] * acc[8] - acc[5] * acc[7]));
+      D[1] = (float)(r * (acc[2] * acc[7] - acc[1] * acc[8]));
+      D[2] = (float)(r * (acc[1] * acc[5] - acc[2] * acc[4]));
+      D[3] = (float)(r * (acc[5] * acc[6] - acc[3] * acc[8]));
+      D[4] = (float)(r * (acc[0] * acc[8] - acc[2] * acc[6]));
+      D[5] = (float)(r * (acc[2] * acc[3] - acc[0] * acc[5]));
+      D[6] = (float)(r * (acc[3] * acc[7] - acc[4] * acc[6]));
+      D[7] = (float)(r * (acc[1] * acc[6] - acc[0] * acc[7]));
+      D[8] = (float)(r * (acc[0] * acc[4] - acc[1] * acc[3]));
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; k++) D[k] = (k % 4 == 0) ? 1.f : 0.f;
+    }
+  }
 }
 
 // ordered gradient sum of vertex v: triangles, stencils (then caller's terms)

@@ -36,6 +36,12 @@ void launch_cg_init(const Arena& A, double tol, int maxit, cudaStream_t s);
 void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, bool serial, cudaStream_t s);
 void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s);
 
+// --- mixed precision (k_mixed.cu) ----------------------------------------------
+void launch_mx_outer_init(const Arena& A, cudaStream_t s);
+void launch_mx_inner_init(const Arena& A, cudaStream_t s);
+void launch_mx_inner_iteration(const Arena& A, int it, float eta, int cap, cudaStream_t s);
+void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s);
+
 // --- collision (k_collide.cu) ------------------------------------------------
 // refit boxes of the active cloths from positions xs (and velocities vs when ccd)
 void launch_refit(const Arena& A, int ccd, const double* xs, const double* vs, double delta_override,

@@ -8,7 +8,8 @@ namespace cs {
 
 const char* const kProfNames[PK_COUNT] = {"tri_elements", "slot_reduce", "rhs",     "ilu_factor",
                                           "pcg",          "cg_spmv",     "cg_update", "cg_direction",
-                                          "refit",        "traverse",    "narrow",    "impulse"};
+                                          "refit",        "traverse",    "narrow",    "impulse",
+                                          "mx_spmv",      "mx_update",   "mx_direction", "mx_residual"};
 
 namespace {
 struct Pending {

@@ -18,6 +18,10 @@ enum ProfKernel {
   PK_TRAVERSE,
   PK_NARROW,
   PK_IMPULSE,
+  PK_MX_SPMV,
+  PK_MX_UPDATE,
+  PK_MX_DIRECTION,
+  PK_MX_RESIDUAL,
   PK_COUNT
 };
 

@@ -1,0 +1,94 @@
+"""Mixed-precision solve (CS_PREC_MIXED): FP32 block-Jacobi CG inside FP64
+iterative refinement.  Bounds: the implicit-step increment meets the
+reference's criterion (relative residual below the tolerance) on the FP64
+system the oracle assembles, and positions after one implicit step agree with
+the FP64 oracle within MIXED_RTOL relative."""
+import numpy as np
+import pytest
+
+from cloth_sim_self_collision_gb300 import scene
+from oracle import oracle as O
+from tests.test_gpu_parity import fold_scene, residual_ratio
+
+pytestmark = pytest.mark.gpu
+
+MIXED_RTOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def mctx():
+    from cloth_sim_self_collision_gb300 import build
+    build.build()
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    c = ClothContext(0, "mixed")
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("name", ["small_21", "fold_31", "batch_61"])
+def test_mixed_implicit_accuracy(mctx, oracle_port, name):
+    if name == "small_21":
+        c = scene.config_small()
+    elif name == "fold_31":
+        c = fold_scene()
+    else:
+        c = scene.square_cloth(61, 1.0, 0.6, sphere_radius=0.25, seed=5, solver_kind=scene.SOLVER_CG,
+                               tol=1e-6, maxit=1000)
+    cid = mctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    rp, ci = orc.pattern()
+    worst = 0.0
+    for f in range(0, 80, 8):
+        x0 = orc.x.copy()
+        vd, vc, b = orc.assemble(orc.x, orc.v)
+        xa, va, sa = mctx.implicit(cid, orc.x, orc.v)
+        xb, vb, sb = orc.implicit(orc.x, orc.v)
+        ra = residual_ratio(vd, vc, rp, ci, b, xa - x0)
+        assert ra < c.params.tol, (name, f, ra)
+        err = np.abs(xa - xb).max() / max(1.0, np.abs(xb).max())
+        worst = max(worst, err)
+        assert err <= MIXED_RTOL, (name, f, err)
+        orc.step(8)
+    print(f"{name}: worst position error after one implicit step {worst:.2e}")
+    mctx.remove_cloth(cid)
+
+
+def test_mixed_frames_contacts(mctx, oracle_port):
+    """Whole frames from oracle states of the folding sheet: positions within
+    MIXED_RTOL and the same contact counts as the FP64 oracle."""
+    c = fold_scene()
+    cid = mctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    frame = 0
+    same = 0
+    frames = [30, 34, 38, 45, 60, 90]
+    for f in frames:
+        orc.step(f - frame)
+        frame = f
+        mctx.set_state(cid, orc.x, orc.v)
+        nxt = O.OracleCloth(oracle_port, c)
+        nxt.x, nxt.v = orc.x.copy(), orc.v.copy()
+        sb = nxt.step(1)[0]
+        mctx.step(1)
+        xa, _ = mctx.get_state(cid)
+        sa = mctx.stats(cid)
+        err = np.abs(xa - nxt.x).max() / max(1.0, np.abs(nxt.x).max())
+        print(f"frame {f}: err {err:.2e} prx {sa['n_prx']}/{sb['n_prx']} ccd {sa['n_ccd']}/{sb['n_ccd']}")
+        same += sa["n_prx"] == sb["n_prx"] and sa["n_ccd"] == sb["n_ccd"]
+        assert err <= 1e-3, (f, err)
+        nxt.close()
+    assert same >= len(frames) - 1
+    mctx.remove_cloth(cid)
+
+
+def test_mixed_batch_runs(mctx):
+    cl = scene.config_batch(count=16)
+    ids = [mctx.add_cloth(c) for c in cl]
+    mctx.step(4)
+    for i in ids:
+        x, v = mctx.get_state(i)
+        assert np.all(np.isfinite(x)) and np.all(np.isfinite(v))
+        st = mctx.stats(i)
+        assert st["solver_conv"] < 1e-6
+    for i in ids:
+        mctx.remove_cloth(i)
