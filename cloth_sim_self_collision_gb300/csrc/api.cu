@@ -346,6 +346,8 @@ void rebuild(cs_ctx* c) {
   A.tri_leaf = m.upload(tri_leaf, s);
   A.refit_cnt = m.alloc<int>(NN);
   A.box = m.alloc<Box>(NN);
+  A.box32 = m.alloc<float>(6 * (size_t)NN);
+  A.vb32 = m.alloc<float>(6 * (size_t)NV);
   A.edge_uv = m.upload(edge_uv, s);
   A.uf = m.alloc<int>(NV);
   A.inzone = m.alloc<int>(NV);
@@ -405,6 +407,8 @@ void rebuild(cs_ctx* c) {
     A.q32 = m.alloc<float>(3 * (size_t)NV);
     A.z32 = m.alloc<float>(3 * (size_t)NV);
     A.part32 = m.alloc<double>(3 * (size_t)std::max(A.nslice, 1));
+    A.red_cnt = m.alloc<int>(std::max(ni, 1));
+    CK(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(ni, 1), s));
     A.mixed = 1;
   }
   c->A = A;

@@ -49,6 +49,7 @@ struct InstState {
   int inner_iters;   // inner iterations of the current inner solve
   int total_iters;   // inner iterations summed over refinement cycles
   int cycles;        // refinement cycles
+  double red[3];     // per-cloth totals of the slice partials: p.q, r.z, r.r
 };
 
 struct Arena {
@@ -82,6 +83,11 @@ struct Arena {
   int *node = nullptr, *pre = nullptr, *skip = nullptr, *leaf_lo = nullptr, *leaf_hi = nullptr;
   int *depth = nullptr, *prepos = nullptr, *tri_leaf = nullptr, *refit_cnt = nullptr, *preoff = nullptr;
   Box* box = nullptr;
+  // FP32 copies rounded outward (they contain the FP64 boxes): 6 floats per node
+  // (lo xyz, hi xyz; an empty box is lo = +inf, hi = -inf) and per vertex (the
+  // point, or its swept box for CCD), for conservative prefilters
+  float* box32 = nullptr;
+  float* vb32 = nullptr;
   // impact zones
   int *edge_uv = nullptr, *uf = nullptr, *inzone = nullptr;
   // mixed precision: FP32 copy of the matrix in warp slices (SELL-32: 32 rows per
@@ -97,6 +103,7 @@ struct Arena {
   float* dinv32 = nullptr;          // 9 per vertex
   float *r32 = nullptr, *d32 = nullptr, *p32 = nullptr, *q32 = nullptr, *z32 = nullptr;
   double* part32 = nullptr;         // 3 per slice: p.q, r.z, r.r
+  int* red_cnt = nullptr;           // per cloth: slices that have written their partials
   int mixed = 0;                    // mixed-precision arrays present
 };
 

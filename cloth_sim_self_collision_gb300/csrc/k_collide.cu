@@ -42,6 +42,24 @@ __device__ __forceinline__ Box load_box(const Box* b, int n) {
   return r;
 }
 
+// outward-rounded FP32 copy of an FP64 box (contains it); empty -> never overlaps
+__device__ __forceinline__ void store_box32(float* dst, const Box& b) {
+  if (!b.full) {
+    dst[0] = dst[1] = dst[2] = __int_as_float(0x7f800000);
+    dst[3] = dst[4] = dst[5] = -__int_as_float(0x7f800000);
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    dst[k] = __double2float_rd(b.lo[k]);
+    dst[3 + k] = __double2float_ru(b.hi[k]);
+  }
+}
+
+__device__ __forceinline__ bool overlap32(const float* a, const float* b) {
+  return !(a[3] < b[0] || a[0] > b[3] || a[4] < b[1] || a[1] > b[4] || a[5] < b[2] || a[2] > b[5]);
+}
+
 __device__ __forceinline__ V3<double> end_pos(const double* x, const double* v, int i, double dt) {
   return mk<double>(x[3 * i + 0] + dt * v[3 * i + 0], x[3 * i + 1] + dt * v[3 * i + 1], x[3 * i + 2] + dt * v[3 * i + 2]);
 }
@@ -69,6 +87,7 @@ __global__ void k_refit(Arena A, int ccd, const double* xs, const double* vs, do
   }
   int n = A.tri_leaf[t];
   A.box[n] = b;
+  store_box32(A.box32 + 6 * (size_t)n, b);
   for (;;) {
     __threadfence();
     const int par = A.node[3 * n + 0];
@@ -77,7 +96,38 @@ __global__ void k_refit(Arena A, int ccd, const double* xs, const double* vs, do
     Box m = load_box(A.box, A.node[3 * par + 1]);
     box_merge(m, load_box(A.box, A.node[3 * par + 2]));
     A.box[par] = m;
+    store_box32(A.box32 + 6 * (size_t)par, m);
     n = par;
+  }
+}
+
+// per vertex FP32 bounds for the prefilters: the point (proximity) or its swept
+// box [min(p-eps, q-eps), max(p+eps, q+eps)], q = p + dt v, eps = 1e-10, with the
+// FP64 rounding of the reference's AddPoint (CCD), rounded outward
+__global__ void k_vertex_bounds(Arena A, int ccd, const double* xs, const double* vs) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  const int inst = A.vinst[v];
+  if (!A.active[inst]) return;
+  float* dst = A.vb32 + 6 * (size_t)v;
+  if (!ccd) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double p = xs[3 * v + k];
+      dst[k] = __double2float_rd(p);
+      dst[3 + k] = __double2float_ru(p);
+    }
+    return;
+  }
+  const double dt = A.prm[inst].dt, eps = 1.0e-10;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double p = xs[3 * v + k];
+    const double q = p + dt * vs[3 * v + k];
+    const double lo = (p - eps < q - eps) ? p - eps : q - eps;
+    const double hi = (p + eps > q + eps) ? p + eps : q + eps;
+    dst[k] = __double2float_rd(lo);
+    dst[3 + k] = __double2float_ru(hi);
   }
 }
 
@@ -184,6 +234,11 @@ __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, cons
     const int tf = fa ? ta : tb, tv = fa ? tb : ta, k = fa ? test : test - 3;
     const int f0 = A.tri[3 * tf], f1 = A.tri[3 * tf + 1], f2 = A.tri[3 * tf + 2], q = A.tri[3 * tv + k];
     if (q == f0 || q == f1 || q == f2) return;
+    // FP32 prefilter: rejects only what the FP64 box test rejects (outward boxes)
+    {
+      const int bn = ccd ? (fa ? na : nb) : A.noff[inst] + (tf - A.toff[inst]);
+      if (!overlap32(A.box32 + 6 * (size_t)bn, A.vb32 + 6 * (size_t)q)) return;
+    }
     const V3<double> p0 = ld3(xs, f0), p1 = ld3(xs, f1), p2 = ld3(xs, f2), p3 = ld3(xs, q);
     if (!ccd) {
       // the reference passes aBB[triangle index]: the box of the node whose
@@ -202,6 +257,33 @@ __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, cons
   const int i0 = A.tri[3 * ta + kEE[k][0]], i1 = A.tri[3 * ta + kEE[k][1]];
   const int j0 = A.tri[3 * tb + kEE[k][2]], j1 = A.tri[3 * tb + kEE[k][3]];
   if (i0 == j0 || i0 == j1 || i1 == j0 || i1 == j1) return;
+  {
+    // FP32 prefilter on outward bounds: for CCD the edges' swept boxes must
+    // overlap; for proximity the reference's six slab tests (bvh_aabb.cpp:420-425)
+    // are bounded with directed rounding, so a rejection here is a rejection in FP64
+    const float *a0 = A.vb32 + 6 * (size_t)i0, *a1 = A.vb32 + 6 * (size_t)i1;
+    const float *b0 = A.vb32 + 6 * (size_t)j0, *b1 = A.vb32 + 6 * (size_t)j1;
+    if (ccd) {
+      float ea[6], eb[6];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        ea[k] = fminf(a0[k], a1[k]);
+        ea[3 + k] = fmaxf(a0[3 + k], a1[3 + k]);
+        eb[k] = fminf(b0[k], b1[k]);
+        eb[3 + k] = fmaxf(b0[3 + k], b1[3 + k]);
+      }
+      if (!overlap32(ea, eb)) return;
+    } else {
+      const float du = __double2float_ru(delta);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float plo = fminf(a0[k], a1[k]), phi = fmaxf(a0[3 + k], a1[3 + k]);
+        const float qlo = fminf(b0[k], b1[k]), qhi = fmaxf(b0[3 + k], b1[3 + k]);
+        if (__fadd_ru(qhi, du) < plo) return;  // q + delta < p for all four combinations
+        if (__fsub_rd(qlo, du) > phi) return;  // q - delta > p for all four combinations
+      }
+    }
+  }
   const V3<double> p0 = ld3(xs, i0), p1 = ld3(xs, i1), q0 = ld3(xs, j0), q1 = ld3(xs, j1);
   if (!ccd) {
     if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
@@ -646,6 +728,8 @@ __global__ void k_riz_labels(Arena A, int* zone_of) {
 // ---- launchers ----------------------------------------------------------------
 void launch_refit(const Arena& A, int ccd, const double* xs, const double* vs, double delta_override,
                   cudaStream_t s) {
+  k_vertex_bounds<<<nblk(A.nv), kT, 0, s>>>(A, ccd, xs, vs);
+  g_launches++;
   cudaMemsetAsync(A.refit_cnt, 0, sizeof(int) * (size_t)A.nn, s);
   prof_begin(PK_REFIT, s);
   k_refit<<<nblk(A.nt), kT, 0, s>>>(A, ccd, xs, vs, delta_override);

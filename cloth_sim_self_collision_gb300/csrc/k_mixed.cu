@@ -35,6 +35,27 @@ __device__ __forceinline__ double cloth_total(const Arena& A, int inst, int fiel
   return warp_sum_d(s);
 }
 
+// The last warp of a cloth to finish (ticket counter) sums the cloth's slice
+// partials [f0, f0 + nf) in slice order into st.red: one pass, deterministic.
+__device__ void finish_cloth(const Arena& A, int inst, int lane, int f0, int nf) {
+  int last = 0;
+  if (lane == 0) {
+    __threadfence();
+    const int n = A.slice_hi[inst] - A.slice_lo[inst];
+    last = (atomicAdd(&A.red_cnt[inst], 1) == n - 1);
+  }
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return;
+  __threadfence();
+  for (int f = f0; f < f0 + nf; f++) {
+    double s = 0.0;
+    for (int k = A.slice_lo[inst] + lane; k < A.slice_hi[inst]; k += 32) s += __ldcg(&A.part32[3 * k + f]);
+    s = warp_sum_d(s);
+    if (lane == 0) A.st[inst].red[f] = s;
+  }
+  if (lane == 0) A.red_cnt[inst] = 0;
+}
+
 __device__ __forceinline__ void apply_dinv(const float* D, const float r[3], float z[3]) {
   z[0] = D[0] * r[0] + D[1] * r[1] + D[2] * r[2];
   z[1] = D[3] * r[0] + D[4] * r[1] + D[5] * r[2];
@@ -127,13 +148,14 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_spmv(Arena A) {
   }
   pq = warp_sum_f(pq);
   if (c.lane == 0) A.part32[3 * c.slice + 0] = pq;
+  finish_cloth(A, c.inst, c.lane, 0, 1);
 }
 
 // alpha = r.z / p.q; d += alpha p; r -= alpha q; z = D^-1 r; partials of r.z, r.r
 __global__ void __launch_bounds__(kSliceThreads) k_mx_update(Arena A, int it) {
   SliceCtx c;
   if (!slice_ctx(A, c, true)) return;
-  const double pq = cloth_total(A, c.inst, 0);
+  const double pq = A.st[c.inst].red[0];
   const float alpha = (float)(A.st[c.inst].rz[it & 1] / pq);
   float rz = 0.f, rr = 0.f;
   if (c.valid) {
@@ -159,6 +181,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_update(Arena A, int it) {
     A.part32[3 * c.slice + 1] = rz;
     A.part32[3 * c.slice + 2] = rr;
   }
+  finish_cloth(A, c.inst, c.lane, 1, 2);
 }
 
 // inner convergence (|r|^2 <= eta^2 |r0|^2 or the cap), beta, p = z + beta p
@@ -166,7 +189,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
   SliceCtx c;
   if (!slice_ctx(A, c, true)) return;
   InstState& S = A.st[c.inst];
-  const double rzn = cloth_total(A, c.inst, 1), rrn = cloth_total(A, c.inst, 2);
+  const double rzn = S.red[1], rrn = S.red[2];
   const bool first = (c.slice == A.slice_lo[c.inst]) && c.lane == 0;
   if (rrn <= (double)eta * (double)eta * S.rr_in0 || it >= cap) {
     if (first) {
@@ -304,7 +327,9 @@ __global__ void k_mx_check(Arena A, double tol_in, int maxcycles) {
   S.cycles += 1;
   S.solver_conv = sqrt(sq * S.inv0);
   S.solver_iterations = S.total_iters;
-  if (sq * S.inv0 < tol * tol || S.cycles >= maxcycles) S.done = 1;
+  // stop one decade below the reference's tolerance: the result then stays
+  // within the reference's own truncation error of the exact solution
+  if (sq * S.inv0 < 0.01 * tol * tol || S.cycles >= maxcycles) S.done = 1;
 }
 
 }  // namespace
