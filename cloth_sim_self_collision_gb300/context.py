@@ -110,6 +110,12 @@ class ClothContext:
     def profile(self, enable: bool):
         self._ck(self.L.cs_profile(self.h, 1 if enable else 0))
 
+    def profile_bytes(self):
+        """(FP32 SpMV bytes, FP64 SpMV bytes) since profiling was enabled."""
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        self._ck(self.L.cs_profile_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def profile_read(self, kernel: str):
         ms = ctypes.c_double()
         n = ctypes.c_longlong()

@@ -327,6 +327,19 @@ void rebuild(cs_ctx* c) {
   A.dx = m.alloc<double>(3 * (size_t)NV);
   CK(cudaMemsetAsync(A.z, 0, sizeof(double) * 3 * (size_t)std::max(NV, 1), s));
   A.part = m.alloc<double>(2 * (size_t)A.nchunk);
+  {
+    std::vector<long long> cb(A.nchunk, 0);
+    for (int k = 0; k < A.nchunk; k++) {
+      const int i = chunk_inst[k];
+      const ClothTopo& t = c->cloths[c->order[i]]->topo;
+      const int r0 = (k - chunk_lo[i]) * 256;
+      for (int l = 0; l < 256 && r0 + l < t.np; l++)
+        cb[k] += 76LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l]) + 72 + 48 + 4;  // blocks + cols, diag, x, y, row ptr
+    }
+    A.chunk_bytes = m.upload(cb, s);
+    A.bytes_acc = m.alloc<unsigned long long>(2);
+    CK(cudaMemsetAsync(A.bytes_acc, 0, 2 * sizeof(unsigned long long), s));
+  }
   A.lev_off = m.upload(lev_off, s);
   A.lev_ptr = m.upload(lev_ptr, s);
   A.lev_rows = m.upload(lev_rows, s);
@@ -407,6 +420,17 @@ void rebuild(cs_ctx* c) {
     A.q32 = m.alloc<float>(3 * (size_t)NV);
     A.z32 = m.alloc<float>(3 * (size_t)NV);
     A.part32 = m.alloc<double>(3 * (size_t)std::max(A.nslice, 1));
+    {
+      std::vector<long long> sb(A.nslice, 0);
+      for (int k = 0; k < A.nslice; k++) {
+        const int i = slice_inst[k];
+        const ClothTopo& t = c->cloths[c->order[i]]->topo;
+        const int r0 = slice_row0[k] - c->voff[i];
+        for (int l = 0; l < 32 && r0 + l < t.np; l++)
+          sb[k] += 40LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l] + 1) + 24;  // blocks + cols, x, y (FP32)
+      }
+      A.slice_bytes = m.upload(sb, s);
+    }
     A.red_cnt = m.alloc<int>(std::max(ni, 1));
     CK(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(ni, 1), s));
     A.mixed = 1;
@@ -1320,9 +1344,24 @@ long long cs_launch_count(const cs_ctx* c) { return c ? g_launches - c->launches
 
 int cs_profile(cs_ctx* c, int enable) {
   return guarded(c, [&] {
+    ensure(c);
     CK(cudaStreamSynchronize(c->stream));
     prof_reset();
     prof_enable(enable != 0);
+    c->A.count_bytes = enable != 0;
+    if (c->A.bytes_acc) CK(cudaMemsetAsync(c->A.bytes_acc, 0, 2 * sizeof(unsigned long long), c->stream));
+  });
+}
+
+int cs_profile_bytes(cs_ctx* c, long long* spmv32, long long* spmv64) {
+  return guarded(c, [&] {
+    ensure(c);
+    unsigned long long h[2] = {0, 0};
+    if (c->A.bytes_acc)
+      CK(cudaMemcpyAsync(h, c->A.bytes_acc, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (spmv32) *spmv32 = (long long)h[0];
+    if (spmv64) *spmv64 = (long long)h[1];
   });
 }
 

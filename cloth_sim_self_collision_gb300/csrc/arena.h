@@ -104,6 +104,12 @@ struct Arena {
   float *r32 = nullptr, *d32 = nullptr, *p32 = nullptr, *q32 = nullptr, *z32 = nullptr;
   double* part32 = nullptr;         // 3 per slice: p.q, r.z, r.r
   int* red_cnt = nullptr;           // per cloth: slices that have written their partials
+  // algorithmic bytes of one SpMV over a slice / chunk (real blocks, column
+  // indices, x once, y once) and their running totals while profiling
+  long long* slice_bytes = nullptr;
+  long long* chunk_bytes = nullptr;
+  unsigned long long* bytes_acc = nullptr;  // [0] FP32 SpMV, [1] FP64 SpMV
+  int count_bytes = 0;
   int mixed = 0;                    // mixed-precision arrays present
 };
 

@@ -147,7 +147,10 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_spmv(Arena A) {
     pq = A.p32[3 * c.row + 0] * y0 + A.p32[3 * c.row + 1] * y1 + A.p32[3 * c.row + 2] * y2;
   }
   pq = warp_sum_f(pq);
-  if (c.lane == 0) A.part32[3 * c.slice + 0] = pq;
+  if (c.lane == 0) {
+    A.part32[3 * c.slice + 0] = pq;
+    if (A.count_bytes) atomicAdd(&A.bytes_acc[0], (unsigned long long)A.slice_bytes[c.slice]);
+  }
   finish_cloth(A, c.inst, c.lane, 0, 1);
 }
 

@@ -369,7 +369,10 @@ __global__ void __launch_bounds__(kChunk) k_cg_spmv(Arena A) {
         A.p[3 * row + 2] * A.z[3 * row + 2];
   }
   s = block_sum(s, sh);
-  if (threadIdx.x == 0) A.part[c] = s;
+  if (threadIdx.x == 0) {
+    A.part[c] = s;
+    if (A.count_bytes) atomicAdd(&A.bytes_acc[1], (unsigned long long)A.chunk_bytes[c]);
+  }
 }
 
 // alpha = r.r / p.Ap; x += alpha p; r -= alpha Ap; chunk partials of r.r

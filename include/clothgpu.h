@@ -216,6 +216,10 @@ long long cs_launch_count(const cs_ctx *ctx);
  * "cg_update", "cg_direction", "impulse"). */
 int cs_profile(cs_ctx *ctx, int enable);
 int cs_profile_read(cs_ctx *ctx, const char *kernel, double *total_ms, long long *launches);
+/* Algorithmic bytes moved by the SpMV kernels since profiling was enabled
+ * (blocks, column indices, x and y once per processed row; converged cloths
+ * excluded): the FP32 inner SpMV and the FP64 CG SpMV. */
+int cs_profile_bytes(cs_ctx *ctx, long long *spmv32, long long *spmv64);
 
 #ifdef __cplusplus
 }
