@@ -157,8 +157,11 @@ def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
     ctx.synchronize()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
     prof = {name: ctx.profile_read(name) for name in profile_names}
-    counts = {k: ctx.profile_read(k)[1] for k in ("pairs", "candidates", "contacts", "detections")}
+    counts = {}
     counts["spmv32_bytes"], counts["spmv64_bytes"] = ctx.profile_bytes()
+    for k in ("pairs", "candidates", "contacts", "detections", "fp64_fv_prx", "fp64_ee_prx", "fp64_fv_ccd",
+              "fp64_ee_ccd"):
+        counts[k] = ctx.profile_read(k)[1]
     ctx.profile(False)
     return step_ms, prof, counts, ctx.launch_count() - launches0
 

@@ -18,6 +18,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIB_DIR = os.path.join(PKG, "lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB = os.path.join(LIB_DIR, "libclothgpu.so")
+DROPIN_LIB = os.path.join(LIB_DIR, "libclothgpu_dropin.so")
+DROPIN_SRC = os.path.join(PKG, "dropin", "clothgpu_dropin.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relaxed-constexpr",
@@ -51,7 +53,9 @@ def _stale() -> bool:
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "clothgpu.h"),
-                                                                 os.path.abspath(__file__)]
+                                                                 os.path.abspath(__file__), DROPIN_SRC]
+    if not os.path.exists(DROPIN_LIB):
+        return True
     return any(os.path.getmtime(d) > t for d in deps)
 
 
@@ -69,8 +73,15 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None)
     if r.returncode != 0:
         raise RuntimeError(f"linking failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the C++ drop-in with the reference's signatures, over the C ABI
+    cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-shared", "-o", DROPIN_LIB + ".tmp", DROPIN_SRC,
+                                                        "-L" + LIB_DIR, "-lclothgpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"building the drop-in failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(DROPIN_LIB + ".tmp", DROPIN_LIB)
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", DROPIN_LIB)
     return LIB
 
 

@@ -87,6 +87,8 @@ struct cs_ctx {
   std::vector<int> solver;  // per slot
   int* d_list = nullptr;    // scratch list of cloth slots
   int token = 0;
+  int last_ncand = 0;  // candidates of the last detection (kept in C.cand)
+  int last_nce = 0;    // contacts of the last detection (in C.ce)
   std::vector<InstState> hst;
   long long launches0 = 0;
 };
@@ -337,8 +339,8 @@ void rebuild(cs_ctx* c) {
         cb[k] += 76LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l]) + 72 + 48 + 4;  // blocks + cols, diag, x, y, row ptr
     }
     A.chunk_bytes = m.upload(cb, s);
-    A.bytes_acc = m.alloc<unsigned long long>(2);
-    CK(cudaMemsetAsync(A.bytes_acc, 0, 2 * sizeof(unsigned long long), s));
+    A.bytes_acc = m.alloc<unsigned long long>(8);
+    CK(cudaMemsetAsync(A.bytes_acc, 0, 8 * sizeof(unsigned long long), s));
   }
   A.lev_off = m.upload(lev_off, s);
   A.lev_ptr = m.upload(lev_ptr, s);
@@ -362,6 +364,9 @@ void rebuild(cs_ctx* c) {
   A.box32 = m.alloc<float>(6 * (size_t)NN);
   A.vb32 = m.alloc<float>(6 * (size_t)NV);
   A.edge_uv = m.upload(edge_uv, s);
+  A.vdirty = m.alloc<int>(NV);
+  A.tdirty = m.alloc<int>(NT);
+  CK(cudaMemsetAsync(A.tdirty, 0, sizeof(int) * (size_t)std::max(NT, 1), s));
   A.uf = m.alloc<int>(NV);
   A.inzone = m.alloc<int>(NV);
   CK(cudaMemsetAsync(A.inzone, 0, sizeof(int) * (size_t)std::max(NV, 1), s));
@@ -509,6 +514,7 @@ void run_mixed(cs_ctx* c, const std::vector<int>& act) {
   const int cap = 300, maxcycles = 12;
   set_active(c, act);
   launch_mx_outer_init(A, c->stream);
+  launch_mx_warm_start(A, c->stream);
   for (int cyc = 0; cyc < maxcycles; cyc++) {
     launch_mx_inner_init(A, c->stream);
     for (int it = 1; it <= cap; it++) {
@@ -566,11 +572,46 @@ void implicit(cs_ctx* c, const std::vector<int>& act) {
 
 // ---- contacts ---------------------------------------------------------------------
 // detection for the active cloths; returns the total number of contacts and
-// leaves per-cloth counts in c->hst
-int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_override) {
+// leaves per-cloth counts in c->hst.  incremental (CCD only): the previous
+// detection's candidates are kept for pairs without a dirty triangle and only
+// leaf pairs with a dirty triangle are tested again; the result is the same as
+// a full detection because a test depends only on x and its vertices' velocities.
+int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_override,
+           bool incremental = false) {
   cudaStream_t s = c->stream;
   launch_refit(c->A, ccd, xs, vs, delta_override, s);
   int cnt[4];
+  if (incremental && ccd) {
+    CK(cudaMemsetAsync(c->C.counters, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(c->C.counters + 3, 0, sizeof(int), s));
+    launch_keep_clean_candidates(c->A, c->C, c->last_ncand, s);
+    launch_traverse_dirty(c->A, c->C, s);
+    CK(cudaMemcpyAsync(cnt, c->C.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    bool ok = !cnt[3];
+    if (ok) {
+      launch_narrow(c->A, c->C, ccd, xs, vs, delta_override, cnt[0], s);
+      CK(cudaMemcpyAsync(cnt, c->C.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      ok = !cnt[3];
+    }
+    if (ok) {
+      const int ncand = cnt[1];
+      sort_dedupe(c->A, c->C, ncand, s);
+      CK(cudaGetLastError());
+      int total = 0;
+      CK(cudaMemcpyAsync(&total, c->C.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+      pull_states(c);
+      prof_count("pairs", cnt[0]);
+      prof_count("candidates", ncand);
+      prof_count("contacts", total);
+      prof_count("detections", 1);
+      c->last_ncand = ncand;
+      c->last_nce = total;
+      return total;
+    }
+    // a buffer overflowed: fall back to a full detection (which grows the buffers)
+  }
   for (int attempt = 0;; attempt++) {
     CK(cudaMemsetAsync(c->C.counters, 0, sizeof(int) * 4, s));
     launch_traverse(c->A, c->C, s);
@@ -604,6 +645,8 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
   prof_count("candidates", ncand);
   prof_count("contacts", total);
   prof_count("detections", 1);
+  c->last_ncand = ncand;
+  c->last_nce = total;
   return total;
 }
 
@@ -642,7 +685,8 @@ std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
     for (int i = 0; i < ni; i++) any |= phase[i] != 0;
     if (!any) break;
     set_active(c, phase);
-    detect(c, 1, A.x1, A.v, -1.0);
+    if (it > 0) launch_mark_dirty(A, c->C, c->last_nce, false, c->stream);
+    detect(c, 1, A.x1, A.v, -1.0, it > 0);
     for (int i = 0; i < ni; i++) {
       if (!phase[i]) continue;
       cs_stats& st = c->cloths[c->order[i]]->stats;
@@ -667,7 +711,10 @@ std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
       for (int i = 0; i < ni; i++) more |= phase[i] != 0;
       if (!more) break;
       set_active(c, phase);
-      detect(c, 1, A.x1, A.v, -1.0);
+      // velocities changed at the last pass's contacts (first pass: the fifth
+      // CCD impulses) or, after a zone pass, at the zone vertices
+      launch_mark_dirty(A, c->C, c->last_nce, it > 0, c->stream);
+      detect(c, 1, A.x1, A.v, -1.0, true);
       launch_riz_count(A, c->stream);
       pull_states(c);
       int nce = 0;
@@ -1087,6 +1134,14 @@ static void boxes_out(cs_ctx* c, int i, int nnode, double* boxes) {
   }
 }
 
+int cs_get_boxes(cs_ctx* c, int id, double* boxes) {
+  return guarded(c, [&] {
+    if (!boxes) throw ArgError("null boxes");
+    ensure(c);
+    boxes_out(c, slot_of(c, id), c->cloths[id]->topo.nnode, boxes);
+  });
+}
+
 int cs_refit_prx(cs_ctx* c, int id, const double* x, double delta, double* boxes) {
   return guarded(c, [&] {
     if (!x) throw ArgError("null positions");
@@ -1349,19 +1404,23 @@ int cs_profile(cs_ctx* c, int enable) {
     prof_reset();
     prof_enable(enable != 0);
     c->A.count_bytes = enable != 0;
-    if (c->A.bytes_acc) CK(cudaMemsetAsync(c->A.bytes_acc, 0, 2 * sizeof(unsigned long long), c->stream));
+    if (c->A.bytes_acc) CK(cudaMemsetAsync(c->A.bytes_acc, 0, 8 * sizeof(unsigned long long), c->stream));
   });
 }
 
 int cs_profile_bytes(cs_ctx* c, long long* spmv32, long long* spmv64) {
   return guarded(c, [&] {
     ensure(c);
-    unsigned long long h[2] = {0, 0};
+    unsigned long long h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (c->A.bytes_acc)
       CK(cudaMemcpyAsync(h, c->A.bytes_acc, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (spmv32) *spmv32 = (long long)h[0];
     if (spmv64) *spmv64 = (long long)h[1];
+    prof_count("fp64_fv_prx", (long long)h[2]);
+    prof_count("fp64_ee_prx", (long long)h[3]);
+    prof_count("fp64_fv_ccd", (long long)h[4]);
+    prof_count("fp64_ee_ccd", (long long)h[5]);
   });
 }
 

@@ -90,6 +90,9 @@ struct Arena {
   float* vb32 = nullptr;
   // impact zones
   int *edge_uv = nullptr, *uf = nullptr, *inzone = nullptr;
+  // incremental CCD re-detection: vertices / triangles whose velocity changed
+  // since the last detection
+  int *vdirty = nullptr, *tdirty = nullptr;
   // mixed precision: FP32 copy of the matrix in warp slices (SELL-32: 32 rows per
   // slice, blocks of a slice stored entry-major so every load is 32 consecutive
   // floats), block-Jacobi inverse, FP32 work vectors
@@ -108,7 +111,8 @@ struct Arena {
   // indices, x once, y once) and their running totals while profiling
   long long* slice_bytes = nullptr;
   long long* chunk_bytes = nullptr;
-  unsigned long long* bytes_acc = nullptr;  // [0] FP32 SpMV, [1] FP64 SpMV
+  unsigned long long* bytes_acc = nullptr;  // [0] FP32 SpMV, [1] FP64 SpMV, [2..5] narrow-phase
+                                            // tests reaching FP64: FV prx, EE prx, FV ccd, EE ccd
   int count_bytes = 0;
   int mixed = 0;                    // mixed-precision arrays present
 };

@@ -172,6 +172,72 @@ __global__ void k_traverse(Arena A, ContactBufs C) {
   }
 }
 
+// every overlapping leaf pair with a dirty triangle, oriented by leaf order; a
+// pair of two dirty triangles is emitted by its left one
+__global__ void k_traverse_dirty(Arena A, ContactBufs C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nt || !A.tdirty[t]) return;
+  const int inst = A.tinst[t];
+  if (!A.active[inst]) return;
+  const int la = A.tri_leaf[t];
+  const int oa = A.leaf_lo[la];
+  const Box ba = A.box[la];
+  int k = A.preoff[inst];
+  const int end = A.preoff[inst + 1];
+  while (k < end) {
+    const int n = A.pre[k];
+    if (!box_overlap(ba, A.box[n])) {
+      k = A.skip[k];
+      continue;
+    }
+    if (A.node[3 * n + 2] == -1) {
+      const int ob = A.leaf_lo[n];
+      const bool other_dirty = A.tdirty[A.node[3 * n + 1]] != 0;
+      if (n != la && (!other_dirty || oa < ob)) {
+        const int slot = warp_append(&C.counters[0]);
+        if (slot < C.pair_cap)
+          C.pairs[slot] = (oa < ob) ? make_int2(la, n) : make_int2(n, la);
+        else
+          C.counters[3] = 1;
+      }
+      k = A.skip[k];
+    } else {
+      k++;
+    }
+  }
+}
+
+// candidates of the previous detection whose pair has no dirty triangle
+__global__ void k_keep_clean(Arena A, ContactBufs C, int ncand, int* nkeep) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncand) return;
+  const Cand c = C.cand[i];
+  const int ta = A.node[3 * c.na + 1], tb = A.node[3 * c.nb + 1];
+  if (A.tdirty[ta] || A.tdirty[tb] || !A.active[A.tinst[ta]]) return;
+  C.cand_sorted[atomicAdd(nkeep, 1)] = c;
+}
+
+__global__ void k_mark_contacts(Arena A, ContactBufs C, int nce) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nce) return;
+  const int* e = C.ce + 5 * c;
+  if (!A.active[A.vinst[e[1]]]) return;
+#pragma unroll
+  for (int k = 1; k <= 4; k++) A.vdirty[e[k]] = 1;
+}
+
+__global__ void k_mark_zones(Arena A) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  if (A.active[A.vinst[v]] && A.inzone[v]) A.vdirty[v] = 1;
+}
+
+__global__ void k_mark_tris(Arena A) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nt) return;
+  A.tdirty[t] = A.vdirty[A.tri[3 * t]] | A.vdirty[A.tri[3 * t + 1]] | A.vdirty[A.tri[3 * t + 2]];
+}
+
 // canonical key (CContactElement constructor, bvh_aabb.h:68-93)
 __device__ __forceinline__ void canonical(int fv, int j0, int j1, int j2, int j3, int k[4]) {
   if (fv) {
@@ -213,6 +279,12 @@ __device__ __forceinline__ void emit(const ContactBufs& C, int fv, int j0, int j
 __constant__ int kEE[9][4] = {{0, 1, 0, 1}, {0, 1, 1, 2}, {0, 1, 2, 0}, {1, 2, 0, 1}, {1, 2, 1, 2},
                               {1, 2, 2, 0}, {2, 0, 0, 1}, {2, 0, 1, 2}, {2, 0, 2, 0}};
 
+__device__ __forceinline__ void count_fp64_test(const Arena& A, int slot) {
+  if (!A.count_bytes) return;
+  const unsigned m = __activemask();
+  if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&A.bytes_acc[slot], (unsigned long long)__popc(m));
+}
+
 // Narrow phase (bvh_aabb.cpp:473-536 proximity, 836-901 CCD): one thread per
 // (elementary test, leaf pair), test-major, so that a warp runs one kind of
 // test (the FP64 paths of the 15 tests differ widely).  Tests 0-2: face a vs
@@ -239,6 +311,7 @@ __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, cons
       const int bn = ccd ? (fa ? na : nb) : A.noff[inst] + (tf - A.toff[inst]);
       if (!overlap32(A.box32 + 6 * (size_t)bn, A.vb32 + 6 * (size_t)q)) return;
     }
+    count_fp64_test(A, ccd ? 4 : 2);
     const V3<double> p0 = ld3(xs, f0), p1 = ld3(xs, f1), p2 = ld3(xs, f2), p3 = ld3(xs, q);
     if (!ccd) {
       // the reference passes aBB[triangle index]: the box of the node whose
@@ -284,6 +357,7 @@ __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, cons
       }
     }
   }
+  count_fp64_test(A, ccd ? 5 : 3);
   const V3<double> p0 = ld3(xs, i0), p1 = ld3(xs, i1), q0 = ld3(xs, j0), q1 = ld3(xs, j1);
   if (!ccd) {
     if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
@@ -742,6 +816,38 @@ void launch_traverse(const Arena& A, const ContactBufs& C, cudaStream_t s) {
   k_traverse<<<nblk(A.nt), kT, 0, s>>>(A, C);
   prof_end(PK_TRAVERSE, s);
   g_launches++;
+}
+
+void launch_traverse_dirty(const Arena& A, const ContactBufs& C, cudaStream_t s) {
+  prof_begin(PK_TRAVERSE, s);
+  k_traverse_dirty<<<nblk(A.nt), kT, 0, s>>>(A, C);
+  prof_end(PK_TRAVERSE, s);
+  g_launches++;
+}
+
+void launch_keep_clean_candidates(const Arena& A, ContactBufs& C, int ncand, cudaStream_t s) {
+  int* nkeep = C.counters + 5;
+  cudaMemsetAsync(nkeep, 0, sizeof(int), s);
+  if (ncand > 0) {
+    k_keep_clean<<<nblk(ncand), kT, 0, s>>>(A, C, ncand, nkeep);
+    g_launches++;
+  }
+  int h = 0;
+  cudaMemcpyAsync(&h, nkeep, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  if (h > 0) cudaMemcpyAsync(C.cand, C.cand_sorted, sizeof(Cand) * (size_t)h, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(C.counters + 1, nkeep, sizeof(int), cudaMemcpyDeviceToDevice, s);
+}
+
+void launch_mark_dirty(const Arena& A, const ContactBufs& C, int nce, bool zones, cudaStream_t s) {
+  cudaMemsetAsync(A.vdirty, 0, sizeof(int) * (size_t)A.nv, s);
+  if (zones) {
+    k_mark_zones<<<nblk(A.nv), kT, 0, s>>>(A);
+  } else if (nce > 0) {
+    k_mark_contacts<<<nblk(nce), kT, 0, s>>>(A, C, nce);
+  }
+  k_mark_tris<<<nblk(A.nt), kT, 0, s>>>(A);
+  g_launches += 2;
 }
 
 void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,

@@ -274,6 +274,16 @@ __global__ void k_mx_outer_start(Arena A) {
   }
 }
 
+// warm start: dx = dt v (the increment of the previous velocity); the stopping
+// criterion stays relative to |b|, the reference's initial residual
+__global__ void k_mx_warm(Arena A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * A.nv) return;
+  const int inst = A.vinst[i / 3];
+  if (!A.active[inst] || A.st[inst].done) return;
+  A.dx[i] = A.bc[i / 3] ? 0.0 : A.prm[inst].dt * A.v[i];
+}
+
 // dx += d (FP64)
 __global__ void k_mx_correct(Arena A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,6 +350,14 @@ __global__ void k_mx_check(Arena A, double tol_in, int maxcycles) {
 void launch_mx_outer_init(const Arena& A, cudaStream_t s) {
   k_mx_outer_init<<<A.nchunk, kChunk, 0, s>>>(A);
   k_mx_outer_start<<<(A.ni + 127) / 128, 128, 0, s>>>(A);
+  g_launches += 2;
+}
+
+void launch_mx_warm_start(const Arena& A, cudaStream_t s) {
+  k_mx_warm<<<(3 * A.nv + 255) / 256, 256, 0, s>>>(A);
+  prof_begin(PK_MX_RESIDUAL, s);
+  k_mx_residual<<<A.nchunk, kChunk, 0, s>>>(A);
+  prof_end(PK_MX_RESIDUAL, s);
   g_launches += 2;
 }
 

@@ -39,6 +39,8 @@ void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s);
 // --- mixed precision (k_mixed.cu) ----------------------------------------------
 void launch_mx_outer_init(const Arena& A, cudaStream_t s);
 void launch_mx_inner_init(const Arena& A, cudaStream_t s);
+// dx = dt v and r = b - A dx (FP64) for the active, unconverged cloths
+void launch_mx_warm_start(const Arena& A, cudaStream_t s);
 void launch_mx_inner_iteration(const Arena& A, int it, float eta, int cap, cudaStream_t s);
 void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s);
 
@@ -47,6 +49,14 @@ void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s)
 void launch_refit(const Arena& A, int ccd, const double* xs, const double* vs, double delta_override,
                   cudaStream_t s);
 void launch_traverse(const Arena& A, const ContactBufs& C, cudaStream_t s);
+// incremental CCD detection: keeps the candidates of pairs whose six vertices
+// kept their velocity (moved to the front of C.cand, count in C.counters[1]) and
+// lists every overlapping leaf pair with a dirty triangle
+void launch_keep_clean_candidates(const Arena& A, ContactBufs& C, int ncand, cudaStream_t s);
+void launch_traverse_dirty(const Arena& A, const ContactBufs& C, cudaStream_t s);
+// dirty marks: the vertices of the current contact list (after impulses) or the
+// zone vertices (after an impact-zone pass); then per triangle
+void launch_mark_dirty(const Arena& A, const ContactBufs& C, int nce, bool zones, cudaStream_t s);
 void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
                    double delta_override, int npairs, cudaStream_t s);
 // sort + deduplicate ncand candidates into C.ce; returns via C.counters[2]

@@ -22,8 +22,9 @@ std::vector<cudaEvent_t> g_free;
 cudaEvent_t g_open[PK_COUNT];
 double g_ms[PK_COUNT];
 long long g_n[PK_COUNT];
-const char* const kCountNames[4] = {"pairs", "candidates", "contacts", "detections"};
-long long g_counts[4];
+const char* const kCountNames[8] = {"pairs", "candidates", "contacts", "detections",
+                                    "fp64_fv_prx", "fp64_ee_prx", "fp64_fv_ccd", "fp64_ee_ccd"};
+long long g_counts[8];
 
 cudaEvent_t get_event() {
   if (!g_free.empty()) {
@@ -76,13 +77,13 @@ void prof_reset() {
 
 void prof_count(const char* name, long long n) {
   if (!g_on) return;
-  for (int k = 0; k < 4; k++)
+  for (int k = 0; k < 8; k++)
     if (std::strcmp(name, kCountNames[k]) == 0) g_counts[k] += n;
 }
 
 bool prof_read(const char* name, double* total_ms, long long* launches) {
   prof_collect();
-  for (int k = 0; k < 4; k++)
+  for (int k = 0; k < 8; k++)
     if (std::strcmp(name, kCountNames[k]) == 0) {
       if (total_ms) *total_ms = 0;
       if (launches) *launches = g_counts[k];

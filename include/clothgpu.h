@@ -186,6 +186,11 @@ int cs_riz_add(cs_ctx *ctx, int id, const int *ce, int n);
 int cs_riz_zones(cs_ctx *ctx, int id, int *zone_of_vertex, int *nzone);
 int cs_riz_apply(cs_ctx *ctx, int id, const double *x, double *v, const double *v0);
 
+/* Boxes of a cloth's BVH from the last refit (the aBB output of
+ * GetIntermidiateVelocityContactResolved, self_collision_cloth.h:33): 7 doubles
+ * per node as in cs_refit_prx. */
+int cs_get_boxes(cs_ctx *ctx, int id, double *boxes);
+
 /* ---- element kernels on batches (cloth_internal_physics.h) --------------------- */
 /* WdWddW_CST (:70-176) for n triangles: C, c [n][9]; W[n], dW[n][9], ddW[n][81] */
 int cs_element_cst(cs_ctx *ctx, int n, const double *C, const double *c, double lambda, double myu,
