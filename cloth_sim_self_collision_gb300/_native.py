@@ -36,7 +36,7 @@ EXPORTS = [
     "cs_contacts_prx", "cs_contacts_ccd", "cs_impulse_prx", "cs_impulse_ccd", "cs_riz_reset", "cs_riz_add",
     "cs_riz_zones", "cs_riz_apply", "cs_element_cst", "cs_element_bend", "cs_element_contact",
     "cs_launch_count", "cs_build_bvh", "cs_build_pattern", "cs_set_states", "cs_get_states", "cs_num_vertices",
-    "cs_profile", "cs_profile_read", "cs_stream", "cs_profile_bytes", "cs_get_boxes",
+    "cs_profile", "cs_profile_read", "cs_stream", "cs_profile_bytes", "cs_get_boxes", "cs_solve_cg_noalloc",
 ]
 
 
@@ -155,6 +155,7 @@ def load(path: str | None = None, build_if_missing: bool = False):
     f("cs_profile", i, _V, i)
     f("cs_stream", _V, _V)
     f("cs_get_boxes", i, _V, i, _D)
+    f("cs_solve_cg_noalloc", i, _V, _V, _V, _V, _V, _V, i, d, i, _D, _I, _V)
     f("cs_profile_bytes", i, _V, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong))
     f("cs_profile_read", i, _V, ctypes.c_char_p, _D, ctypes.POINTER(ctypes.c_longlong))
     _lib = L

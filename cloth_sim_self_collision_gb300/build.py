@@ -25,7 +25,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17"]
-SOURCES = ["topology.cpp", "prof.cu", "k_assemble.cu", "k_solve.cu", "k_mixed.cu", "k_collide.cu", "api.cu"]
+SOURCES = ["topology.cpp", "prof.cu", "k_assemble.cu", "k_solve.cu", "k_mixed.cu", "k_collide.cu", "api.cu",
+           "k_noalloc.cu"]
 
 
 def nvcc() -> str:

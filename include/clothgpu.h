@@ -211,6 +211,26 @@ int cs_get_states(cs_ctx *ctx, double *x, double *v);
 /* Total vertices of the context (length of the state arrays / 3). */
 long long cs_num_vertices(const cs_ctx *ctx);
 
+/* ---- a solve that allocates nothing ---------------------------------------------- */
+/* Maximum block rows (vertices) accepted by cs_solve_cg_noalloc. */
+#define CS_NOALLOC_MAX_VERTICES 16384
+/* No counterpart in the reference: Solve_CG (matrix_square_sparse.cpp:338-406
+ * semantics) for callers that cannot allocate device memory, such as an engine
+ * that owns all device memory through its own pool, or a real-time loop that
+ * must not enter the CUDA allocator.  The caller passes the 3x3 block system in
+ * device memory (row_ptr[np+1], col_idx[nb], vcrs[9 nb], vdia[9 np], b[3 np])
+ * and the device output x[3 np]; conv and iter are host outputs.  No
+ * allocation is made: the work vectors live in one fixed file-scope device array
+ * sized for CS_NOALLOC_MAX_VERTICES rows (about 1.2 MB), which every GPU that
+ * loads the library holds until the process exits.  Larger systems return
+ * CS_ERR_CAPACITY.  The first call on a device looks up that array's device
+ * address (make it before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU race, so serialise them.  Runs on `stream`
+ * (a cudaStream_t, null for the default stream) and waits for it. */
+int cs_solve_cg_noalloc(const int *row_ptr, const int *col_idx, const double *vcrs, const double *vdia,
+                        const double *b, double *x, int np, double tol, int maxit, double *conv, int *iter,
+                        void *stream);
+
 /* ---- counters ------------------------------------------------------------------ */
 /* Kernel launches issued by this context since creation (for launch accounting). */
 long long cs_launch_count(const cs_ctx *ctx);
