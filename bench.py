@@ -160,14 +160,15 @@ def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
     counts = {}
     counts["spmv32_bytes"], counts["spmv64_bytes"] = ctx.profile_bytes()
     for k in ("pairs", "candidates", "contacts", "detections", "fp64_fv_prx", "fp64_ee_prx", "fp64_fv_ccd",
-              "fp64_ee_ccd"):
+              "fp64_ee_ccd", "persist_bytes"):
         counts[k] = ctx.profile_read(k)[1]
     ctx.profile(False)
     return step_ms, prof, counts, ctx.launch_count() - launches0
 
 
 PROFILED = ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit", "traverse",
-            "narrow", "impulse", "pcg", "ilu_factor", "mx_spmv", "mx_update", "mx_direction", "mx_residual")
+            "narrow", "impulse", "pcg", "ilu_factor", "mx_spmv", "mx_update", "mx_direction", "mx_residual",
+            "mx_persist")
 
 
 def plain_one_per_launch(cloths, device, frames: int, budget_s: float = 8.0) -> dict:
@@ -268,16 +269,20 @@ def native(args):
     if not args.no_plain:
         plain = plain_one_per_launch(cloths, local, frames=3)
 
-    # Roofline: the solver's SpMV (HBM-bound) with its algorithmic bytes counted on
-    # the device per processed row; the kernel with the largest share is reported
+    # Roofline: the solver kernel (HBM-bound; in mixed precision the persistent inner
+    # CG, one launch per refinement cycle) with its algorithmic bytes counted on the
+    # device per processed tile / row; the kernel with the largest share is reported
     # beside it (the FP64 narrow phase is bound by the FP64 pipe, not by HBM).
     prof = head["prof"]
     top = max(prof, key=lambda k: prof[k][0])
     total_kernel_ms = sum(v[0] for v in prof.values())
     peaks = read_peaks()
-    spmv = "mx_spmv" if results["headline"] == "mixed" else "cg_spmv"
+    if results["headline"] == "mixed":
+        spmv = "mx_persist" if prof["mx_persist"][1] else "mx_spmv"
+    else:
+        spmv = "cg_spmv"
     ms, n = prof[spmv]
-    alg = head["counts"]["spmv32_bytes" if spmv == "mx_spmv" else "spmv64_bytes"]
+    alg = head["counts"][{"mx_persist": "persist_bytes", "mx_spmv": "spmv32_bytes", "cg_spmv": "spmv64_bytes"}[spmv]]
     roof = {"kernel": spmv, "bound": "hbm", "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "peak_source": peaks["source"], "launches": n, "avg_launch_us": 1e3 * ms / max(n, 1),
             "bytes_per_launch": alg / max(n, 1), "traffic": None,

@@ -37,6 +37,8 @@ EXPORTS = [
     "cs_riz_zones", "cs_riz_apply", "cs_element_cst", "cs_element_bend", "cs_element_contact",
     "cs_launch_count", "cs_build_bvh", "cs_build_pattern", "cs_set_states", "cs_get_states", "cs_num_vertices",
     "cs_profile", "cs_profile_read", "cs_stream", "cs_profile_bytes", "cs_get_boxes", "cs_solve_cg_noalloc",
+    "cs_server_create", "cs_server_submit", "cs_server_wait", "cs_server_release", "cs_server_drain",
+    "cs_server_get_stats", "cs_server_last_error", "cs_server_destroy", "cs_scene_device_bytes",
 ]
 
 
@@ -82,6 +84,36 @@ class CsStats(ctypes.Structure):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["n_ccd"] = list(self.n_ccd)
         return d
+
+
+class CsServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("precision", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_double),
+                ("max_cloths", ctypes.c_int)]
+
+
+class CsRequestInfo(ctypes.Structure):
+    _fields_ = [("np", ctypes.c_int), ("nsteps", ctypes.c_int), ("steps_done", ctypes.c_int),
+                ("status", ctypes.c_int), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
+                ("t_first_frame", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("step_ms_p50", ctypes.c_double), ("step_ms_p99", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CsServerStats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_longlong), ("vertex_steps", ctypes.c_longlong),
+                ("submitted", ctypes.c_int), ("finished", ctypes.c_int), ("queued", ctypes.c_int),
+                ("resident", ctypes.c_int), ("rebuilds", ctypes.c_int),
+                ("elapsed_s", ctypes.c_double), ("busy_s", ctypes.c_double),
+                ("step_ms_p50", ctypes.c_double), ("step_ms_p99", ctypes.c_double),
+                ("step_ms_max", ctypes.c_double), ("admit_ms_p50", ctypes.c_double),
+                ("admit_ms_p99", ctypes.c_double), ("build_ms_total", ctypes.c_double),
+                ("install_ms_total", ctypes.c_double), ("arena_bytes", ctypes.c_double),
+                ("peak_bytes", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -158,6 +190,15 @@ def load(path: str | None = None, build_if_missing: bool = False):
     f("cs_solve_cg_noalloc", i, _V, _V, _V, _V, _V, _V, i, d, i, _D, _I, _V)
     f("cs_profile_bytes", i, _V, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong))
     f("cs_profile_read", i, _V, ctypes.c_char_p, _D, ctypes.POINTER(ctypes.c_longlong))
+    f("cs_server_create", i, ctypes.POINTER(CsServerConfig), ctypes.POINTER(_V))
+    f("cs_server_submit", i, _V, i, _D, _I, i, _I, i, _I, _D, _D, P, i, _I)
+    f("cs_server_wait", i, _V, i, d, _D, _D, ctypes.POINTER(CsRequestInfo))
+    f("cs_server_release", i, _V, i)
+    f("cs_server_drain", i, _V, d)
+    f("cs_server_get_stats", i, _V, ctypes.POINTER(CsServerStats))
+    f("cs_server_last_error", ctypes.c_char_p, _V)
+    f("cs_server_destroy", None, _V)
+    f("cs_scene_device_bytes", ctypes.c_size_t, i, _D, i, _I, i, _I, P)
     _lib = L
     return L
 

@@ -3,6 +3,7 @@
 // (self_contact_sparse/main.cpp:213-263).
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -10,90 +11,12 @@
 #include <string>
 #include <vector>
 
-#include "../../include/clothgpu.h"
-#include "kernels.h"
-#include "topology.h"
+#include "ctx.h"
 
 using namespace cs;
 
-namespace {
-
-struct CudaError : std::runtime_error {
-  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
-};
-struct ArgError : std::runtime_error {
-  explicit ArgError(const std::string& s) : std::runtime_error(s) {}
-};
-struct CapacityError : std::runtime_error {
-  explicit CapacityError(const std::string& s) : std::runtime_error(s) {}
-};
-
-#define CK(expr)                                                                                  \
-  do {                                                                                            \
-    cudaError_t e_ = (expr);                                                                      \
-    if (e_ != cudaSuccess)                                                                        \
-      throw CudaError(std::string(#expr) + ": " + cudaGetErrorString(e_) + " (" __FILE__ ":" +   \
-                      std::to_string(__LINE__) + ")");                                            \
-  } while (0)
-
-struct Cloth {
-  int id = 0;
-  ClothTopo topo;
-  cs_params prm{};
-  std::vector<double> x, v;  // host copy, authoritative only while the arena is rebuilt
-  cs_stats stats{};
-};
-
-// device allocation with ownership in the context
-struct DevMem {
-  std::vector<void*> ptrs;
-  template <typename T>
-  T* alloc(size_t n) {
-    void* p = nullptr;
-    if (n == 0) n = 1;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
-    if (e != cudaSuccess) throw CudaError(std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    ptrs.push_back(p);
-    return (T*)p;
-  }
-  template <typename T>
-  T* upload(const std::vector<T>& h, cudaStream_t s) {
-    T* d = alloc<T>(h.size());
-    if (!h.empty()) CK(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-    return d;
-  }
-  void release() {
-    for (void* p : ptrs) cudaFree(p);
-    ptrs.clear();
-  }
-};
-
-}  // namespace
-
-struct cs_ctx {
-  int device = 0;
-  int precision = CS_PREC_FP64;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  std::map<int, std::unique_ptr<Cloth>> cloths;
-  std::vector<int> order;  // arena slot -> cloth id
-  int next_id = 0;
-  bool dirty = true;
-  Arena A;
-  ContactBufs C;
-  DevMem mem, cmem;  // arena / contact buffers
-  // host mirrors of arena offsets
-  std::vector<int> voff, toff, boff, noff, qoff;
-  std::vector<int> solver;  // per slot
-  int* d_list = nullptr;    // scratch list of cloth slots
-  int token = 0;
-  int last_ncand = 0;  // candidates of the last detection (kept in C.cand)
-  int last_nce = 0;    // contacts of the last detection (in C.ce)
-  std::vector<InstState> hst;
-  long long launches0 = 0;
-};
-
-namespace {
+namespace cs {
+namespace host {
 
 int slot_of(cs_ctx* c, int id) {
   for (size_t i = 0; i < c->order.size(); i++)
@@ -113,11 +36,7 @@ void free_contacts(cs_ctx* c) {
   c->C = ContactBufs();
 }
 
-void alloc_contacts(cs_ctx* c, int pair_cap, int cand_cap) {
-  free_contacts(c);
-  const Arena& A = c->A;
-  ContactBufs& C = c->C;
-  DevMem& m = c->cmem;
+void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t s, int pair_cap, int cand_cap) {
   C.pair_cap = pair_cap;
   C.cand_cap = cand_cap;
   C.ce_cap = cand_cap;
@@ -142,43 +61,49 @@ void alloc_contacts(cs_ctx* c, int pair_cap, int cand_cap) {
   C.zrec = m.alloc<double>(9 * (size_t)A.nv);
   C.cub_bytes = cub_sort_bytes(std::max(cand_cap, A.nv));
   C.cub_tmp = m.alloc<char>(C.cub_bytes);
-  CK(cudaMemsetAsync(C.vstamp, 0xff, sizeof(int) * (size_t)A.nv, c->stream));
-  CK(cudaMemsetAsync(C.counters, 0, sizeof(int) * 8, c->stream));
+  CK(cudaMemsetAsync(C.vstamp, 0xff, sizeof(int) * (size_t)A.nv, s));
+  CK(cudaMemsetAsync(C.counters, 0, sizeof(int) * 8, s));
+}
+
+void alloc_contacts(cs_ctx* c, int pair_cap, int cand_cap) {
+  free_contacts(c);
+  alloc_contacts_into(c->A, c->C, c->cmem, c->stream, pair_cap, cand_cap);
   c->token = 0;
 }
 
-// Rebuilds the device arena from the cloths, keeping their states.
-void rebuild(cs_ctx* c) {
-  // save resident states
-  if (!c->dirty) return;
-  c->mem.release();
-  free_contacts(c);
+// Packs the cloths cl (in this order) into a fresh device arena o on stream s:
+// global indices, slot lists, BVH, SELL slices, and the cloths' host states.
+// Reads only the cloths, so it may run on another thread while a context
+// steps its current arena.
+void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t s) {
   Arena A;
-  const int ni = (int)c->order.size();
+  const int ni = (int)cl.size();
+  o.order.clear();
+  for (const Cloth* k : cl) o.order.push_back(k->id);
   A.ni = ni;
-  c->voff.assign(ni + 1, 0);
-  c->toff.assign(ni + 1, 0);
-  c->qoff.assign(ni + 1, 0);
-  c->boff.assign(ni + 1, 0);
-  c->noff.assign(ni + 1, 0);
-  c->solver.assign(ni, 0);
+  o.voff.assign(ni + 1, 0);
+  o.toff.assign(ni + 1, 0);
+  o.qoff.assign(ni + 1, 0);
+  o.boff.assign(ni + 1, 0);
+  o.noff.assign(ni + 1, 0);
+  o.solver.assign(ni, 0);
   std::vector<int> eoff(ni + 1, 0), chunk_off(ni + 1, 0);
   for (int i = 0; i < ni; i++) {
-    const ClothTopo& t = c->cloths[c->order[i]]->topo;
-    c->voff[i + 1] = c->voff[i] + t.np;
-    c->toff[i + 1] = c->toff[i] + t.nt;
-    c->qoff[i + 1] = c->qoff[i] + t.nq;
-    c->boff[i + 1] = c->boff[i] + t.nb;
-    c->noff[i + 1] = c->noff[i] + t.nnode;
+    const ClothTopo& t = cl[i]->topo;
+    o.voff[i + 1] = o.voff[i] + t.np;
+    o.toff[i + 1] = o.toff[i] + t.nt;
+    o.qoff[i + 1] = o.qoff[i] + t.nq;
+    o.boff[i + 1] = o.boff[i] + t.nb;
+    o.noff[i + 1] = o.noff[i] + t.nnode;
     eoff[i + 1] = eoff[i] + (int)t.edge_uv.size() / 2;
     chunk_off[i + 1] = chunk_off[i] + (t.np + 255) / 256;
-    c->solver[i] = c->cloths[c->order[i]]->prm.solver_kind;
+    o.solver[i] = cl[i]->prm.solver_kind;
   }
-  A.nv = c->voff[ni];
-  A.nt = c->toff[ni];
-  A.nq = c->qoff[ni];
-  A.nb = c->boff[ni];
-  A.nn = c->noff[ni];
+  A.nv = o.voff[ni];
+  A.nt = o.toff[ni];
+  A.nq = o.qoff[ni];
+  A.nb = o.boff[ni];
+  A.nn = o.noff[ni];
   A.ne = eoff[ni];
   A.nchunk = chunk_off[ni];
   const int NV = A.nv, NT = A.nt, NQ = A.nq, NB = A.nb, NN = A.nn;
@@ -192,13 +117,13 @@ void rebuild(cs_ctx* c) {
   std::vector<DevParams> prm;
   X0.reserve(3 * (size_t)NV);
   for (int i = 0; i < ni; i++) {
-    const Cloth& cl = *c->cloths[c->order[i]];
-    const ClothTopo& t = cl.topo;
-    const int vo = c->voff[i], to = c->toff[i], qo = c->qoff[i], bo = c->boff[i], no = c->noff[i];
-    prm.push_back(to_dev(cl.prm));
+    const Cloth& ci = *cl[i];
+    const ClothTopo& t = ci.topo;
+    const int vo = o.voff[i], to = o.toff[i], qo = o.qoff[i], bo = o.boff[i], no = o.noff[i];
+    prm.push_back(to_dev(ci.prm));
     X0.insert(X0.end(), t.X0.begin(), t.X0.end());
-    x.insert(x.end(), cl.x.begin(), cl.x.end());
-    v.insert(v.end(), cl.v.begin(), cl.v.end());
+    x.insert(x.end(), ci.x.begin(), ci.x.end());
+    v.insert(v.end(), ci.v.begin(), ci.v.end());
     bc.insert(bc.end(), t.bc.begin(), t.bc.end());
     vinst.insert(vinst.end(), t.np, i);
     for (int k : t.tri) tri.push_back(k + vo);
@@ -258,17 +183,17 @@ void rebuild(cs_ctx* c) {
   row_ptr.push_back(NB);
   // slot lists: every cloth's off-diagonal slots, then every cloth's diagonal slots
   auto glob = [&](int i, int code, int per_tri, int per_quad) {
-    return code >= 0 ? code + c->toff[i] * per_tri : -((-code - 1) + c->qoff[i] * per_quad) - 1;
+    return code >= 0 ? code + o.toff[i] * per_tri : -((-code - 1) + o.qoff[i] * per_quad) - 1;
   };
   for (int i = 0; i < ni; i++) {
-    const ClothTopo& t = c->cloths[c->order[i]]->topo;
+    const ClothTopo& t = cl[i]->topo;
     for (int s = 0; s < t.nb; s++) {
       for (int e = t.slot_ptr[s]; e < t.slot_ptr[s + 1]; e++) slot_src.push_back(glob(i, t.slot_src[e], 9, 16));
       slot_ptr.push_back((int)slot_src.size());
     }
   }
   for (int i = 0; i < ni; i++) {
-    const ClothTopo& t = c->cloths[c->order[i]]->topo;
+    const ClothTopo& t = cl[i]->topo;
     for (int s = t.nb; s < t.nb + t.np; s++) {
       for (int e = t.slot_ptr[s]; e < t.slot_ptr[s + 1]; e++) slot_src.push_back(glob(i, t.slot_src[e], 9, 16));
       slot_ptr.push_back((int)slot_src.size());
@@ -278,15 +203,14 @@ void rebuild(cs_ctx* c) {
       grad_ptr.push_back((int)grad_src.size());
     }
   }
-  cudaStream_t s = c->stream;
-  DevMem& m = c->mem;
+  DevMem& m = o.mem;
   std::vector<int> ones(ni, 1);
   A.active = m.upload(ones, s);
-  A.voff = m.upload(c->voff, s);
-  A.toff = m.upload(c->toff, s);
-  A.qoff = m.upload(c->qoff, s);
-  A.boff = m.upload(c->boff, s);
-  A.noff = m.upload(c->noff, s);
+  A.voff = m.upload(o.voff, s);
+  A.toff = m.upload(o.toff, s);
+  A.qoff = m.upload(o.qoff, s);
+  A.boff = m.upload(o.boff, s);
+  A.noff = m.upload(o.noff, s);
   A.preoff = A.noff;
   A.chunk_lo = m.upload(chunk_lo, s);
   A.chunk_hi = m.upload(chunk_hi, s);
@@ -333,7 +257,7 @@ void rebuild(cs_ctx* c) {
     std::vector<long long> cb(A.nchunk, 0);
     for (int k = 0; k < A.nchunk; k++) {
       const int i = chunk_inst[k];
-      const ClothTopo& t = c->cloths[c->order[i]]->topo;
+      const ClothTopo& t = cl[i]->topo;
       const int r0 = (k - chunk_lo[i]) * 256;
       for (int l = 0; l < 256 && r0 + l < t.np; l++)
         cb[k] += 76LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l]) + 72 + 48 + 4;  // blocks + cols, diag, x, y, row ptr
@@ -370,7 +294,7 @@ void rebuild(cs_ctx* c) {
   A.uf = m.alloc<int>(NV);
   A.inzone = m.alloc<int>(NV);
   CK(cudaMemsetAsync(A.inzone, 0, sizeof(int) * (size_t)std::max(NV, 1), s));
-  c->d_list = m.alloc<int>(std::max(ni, 1));
+  o.d_list = m.alloc<int>(std::max(ni, 1));
   // mixed precision: SELL-32 slices of every cloth's rows (32 rows per slice,
   // padded to the widest row with zero blocks pointing at the slice's own row)
   {
@@ -378,8 +302,8 @@ void rebuild(cs_ctx* c) {
     std::vector<long long> slice_voff, slice_coff, sell_pos((size_t)NB + NV);
     long long vtot = 0, ctot = 0;
     for (int i = 0; i < ni; i++) {
-      const ClothTopo& t = c->cloths[c->order[i]]->topo;
-      const int vo = c->voff[i], bo = c->boff[i];
+      const ClothTopo& t = cl[i]->topo;
+      const int vo = o.voff[i], bo = o.boff[i];
       slice_lo[i] = (int)slice_inst.size();
       for (int r0 = 0; r0 < t.np; r0 += 32) {
         const int n = std::min(32, t.np - r0);
@@ -429,8 +353,8 @@ void rebuild(cs_ctx* c) {
       std::vector<long long> sb(A.nslice, 0);
       for (int k = 0; k < A.nslice; k++) {
         const int i = slice_inst[k];
-        const ClothTopo& t = c->cloths[c->order[i]]->topo;
-        const int r0 = slice_row0[k] - c->voff[i];
+        const ClothTopo& t = cl[i]->topo;
+        const int r0 = slice_row0[k] - o.voff[i];
         for (int l = 0; l < 32 && r0 + l < t.np; l++)
           sb[k] += 40LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l] + 1) + 24;  // blocks + cols, x, y (FP32)
       }
@@ -438,15 +362,63 @@ void rebuild(cs_ctx* c) {
     }
     A.red_cnt = m.alloc<int>(std::max(ni, 1));
     CK(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(ni, 1), s));
+    // persistent inner solve: algorithmic bytes of one iteration over a slice
+    // (blocks and columns; p_prev, z, p, q in phase A; d, p, q, r, D^-1, z in phase B)
+    {
+      std::vector<long long> pb(A.nslice, 0);
+      for (int k = 0; k < A.nslice; k++) {
+        const int i = slice_inst[k];
+        const ClothTopo& t = cl[i]->topo;
+        const int r0 = slice_row0[k] - o.voff[i];
+        for (int l = 0; l < 32 && r0 + l < t.np; l++)
+          pb[k] += 40LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l] + 1) + 168;
+      }
+      A.slice_pbytes = m.upload(pb, s);
+      A.p32b = m.alloc<float>(3 * (size_t)NV);
+      A.grid_bar = m.alloc<unsigned int>(4);
+      CK(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s));
+    }
     A.mixed = 1;
   }
-  c->A = A;
+  o.A = A;
   if (ni > 0) launch_quad_factors(A, s);
-  alloc_contacts(c, 16 * NT + 4096, 4 * NT + 4096);
+  alloc_contacts_into(o.A, o.C, o.cmem, s, 16 * NT + 4096, 4 * NT + 4096);
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
-  c->hst.assign(ni, InstState());
+  o.hst.assign(ni, InstState());
+}
+
+// Makes o the context's arena; the previous arena's buffers end up in o.
+void install(cs_ctx* c, ArenaSet& o) {
+  std::swap(c->A, o.A);
+  std::swap(c->C, o.C);
+  std::swap(c->mem, o.mem);
+  std::swap(c->cmem, o.cmem);
+  std::swap(c->order, o.order);
+  std::swap(c->voff, o.voff);
+  std::swap(c->toff, o.toff);
+  std::swap(c->qoff, o.qoff);
+  std::swap(c->boff, o.boff);
+  std::swap(c->noff, o.noff);
+  std::swap(c->solver, o.solver);
+  std::swap(c->d_list, o.d_list);
+  std::swap(c->hst, o.hst);
+  c->token = 0;
+  c->last_ncand = 0;
+  c->last_nce = 0;
   c->dirty = false;
+}
+
+// Rebuilds the device arena from c->order, keeping the cloths' (saved) states.
+void rebuild(cs_ctx* c) {
+  if (!c->dirty) return;
+  c->mem.release();
+  free_contacts(c);
+  std::vector<const Cloth*> cl;
+  for (int id : c->order) cl.push_back(c->cloths[id].get());
+  ArenaSet o;
+  build_arena(o, cl, c->stream);
+  install(c, o);
 }
 
 // copies resident states back to the cloths before the arena changes
@@ -516,19 +488,26 @@ void run_mixed(cs_ctx* c, const std::vector<int>& act) {
   launch_mx_outer_init(A, c->stream);
   launch_mx_warm_start(A, c->stream);
   for (int cyc = 0; cyc < maxcycles; cyc++) {
-    launch_mx_inner_init(A, c->stream);
-    for (int it = 1; it <= cap; it++) {
-      launch_mx_inner_iteration(A, it, eta, cap, c->stream);
-      if (it % 8 == 0) {
-        pull_states(c);
-        bool all = true;
-        for (int i = 0; i < A.ni; i++)
-          if (act[i] && !c->hst[i].done && !c->hst[i].idone) all = false;
-        if (all) break;
+    unsigned gave_up = 0;
+    if (c->mx_persistent) {
+      launch_mx_inner_persistent(A, eta, cap, c->mx_blocks_per_sm, c->stream);
+      CK(cudaMemcpyAsync(&gave_up, A.grid_bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    } else {
+      launch_mx_inner_init(A, c->stream);
+      for (int it = 1; it <= cap; it++) {
+        launch_mx_inner_iteration(A, it, eta, cap, c->stream);
+        if (it % 8 == 0) {
+          pull_states(c);
+          bool all = true;
+          for (int i = 0; i < A.ni; i++)
+            if (act[i] && !c->hst[i].done && !c->hst[i].idone) all = false;
+          if (all) break;
+        }
       }
     }
     launch_mx_refine(A, -1.0, maxcycles, c->stream);
     pull_states(c);
+    if (gave_up) throw CudaError("mixed inner solve: a grid barrier wait ran out");
     bool all = true;
     for (int i = 0; i < A.ni; i++)
       if (act[i] && !c->hst[i].done) all = false;
@@ -571,6 +550,11 @@ void implicit(cs_ctx* c, const std::vector<int>& act) {
 }
 
 // ---- contacts ---------------------------------------------------------------------
+// largest pair / candidate buffers (2 GB of leaf pairs, 4 GB of candidates): a
+// detection that needs more fails with CS_ERR_CAPACITY instead of growing on
+constexpr long long kMaxPairs = 1LL << 28;
+constexpr long long kMaxCandidates = 1LL << 25;
+
 // detection for the active cloths; returns the total number of contacts and
 // leaves per-cloth counts in c->hst.  incremental (CCD only): the previous
 // detection's candidates are kept for pairs without a dirty triangle and only
@@ -618,8 +602,12 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
     CK(cudaMemcpyAsync(cnt, c->C.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (!cnt[3]) break;
-    if (attempt > 4) throw CapacityError("broad-phase pair buffer keeps overflowing");
-    alloc_contacts(c, (int)std::min<long long>(2LL * cnt[0] + 4096, 0x7fffffffLL / 2), c->C.cand_cap);
+    // with the overflow flag set, a count below the capacity means the counter wrapped
+    const long long need = (long long)(unsigned)cnt[0];
+    if (attempt > 4 || need > kMaxPairs || need < c->C.pair_cap)
+      throw CapacityError("broad phase: more than " + std::to_string(kMaxPairs) +
+                          " overlapping leaf pairs (boxes of a cloth overlap almost everywhere)");
+    alloc_contacts(c, (int)std::min(2 * need + 4096, kMaxPairs), c->C.cand_cap);
   }
   const int npairs = cnt[0];
   for (int attempt = 0;; attempt++) {
@@ -628,10 +616,12 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
     CK(cudaMemcpyAsync(cnt, c->C.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (!cnt[3]) break;
-    if (attempt > 4) throw CapacityError("contact candidate buffer keeps overflowing");
+    const long long need = (long long)(unsigned)cnt[1];
+    if (attempt > 4 || need > kMaxCandidates || need < c->C.cand_cap)
+      throw CapacityError("narrow phase: more than " + std::to_string(kMaxCandidates) + " contact candidates");
     const int pairs_keep = c->C.pair_cap;
     // the pair list must survive the regrow: recompute it after growing
-    alloc_contacts(c, pairs_keep, (int)std::min<long long>(2LL * cnt[1] + 4096, 0x7fffffffLL / 8));
+    alloc_contacts(c, pairs_keep, (int)std::min(2 * need + 4096, kMaxCandidates));
     CK(cudaMemsetAsync(c->C.counters, 0, sizeof(int) * 4, s));
     launch_traverse(c->A, c->C, s);
   }
@@ -787,25 +777,66 @@ void down(cs_ctx* c, double* dst, const double* src, size_t n) {
   CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
 }
 
+int status_of(const std::exception& e, std::string* msg) {
+  if (msg) *msg = e.what();
+  if (dynamic_cast<const CapacityError*>(&e)) return CS_ERR_CAPACITY;
+  if (dynamic_cast<const CudaError*>(&e))
+    return std::string(e.what()).find("out of memory") != std::string::npos ? CS_ERR_OOM : CS_ERR_CUDA;
+  return CS_ERR_ARG;
+}
+
 template <typename F>
 int guarded(cs_ctx* c, F&& f) {
   if (!c) return CS_ERR_ARG;
   try {
     f();
     return CS_OK;
-  } catch (const ArgError& e) {
-    c->err = e.what();
-    return CS_ERR_ARG;
-  } catch (const CapacityError& e) {
-    c->err = e.what();
-    return CS_ERR_CAPACITY;
-  } catch (const CudaError& e) {
-    c->err = e.what();
-    return std::string(e.what()).find("out of memory") != std::string::npos ? CS_ERR_OOM : CS_ERR_CUDA;
   } catch (const std::exception& e) {
-    c->err = e.what();
-    return CS_ERR_ARG;
+    return status_of(e, &c->err);
   }
+}
+
+std::unique_ptr<Cloth> make_cloth(int np, const double* X0, const int* bc, int nt, const int* tri, int nq,
+                                  const int* quad, const cs_params* prm) {
+  if (np <= 0 || nt <= 0 || nq < 0 || !X0 || !tri || (nq > 0 && !quad) || !prm)
+    throw ArgError("bad sizes or null arrays");
+  if (prm->solver_kind != CS_SOLVER_ILU_PCG && prm->solver_kind != CS_SOLVER_CG) throw ArgError("unknown solver");
+  if (prm->obstacle_kind < 0 || prm->obstacle_kind > 3) throw ArgError("unknown obstacle");
+  for (int k = 0; k < 3 * nt; k++)
+    if (tri[k] < 0 || tri[k] >= np) throw ArgError("triangle index out of range");
+  for (int k = 0; k < 4 * nq; k++)
+    if (quad[k] < 0 || quad[k] >= np) throw ArgError("stencil index out of range");
+  std::unique_ptr<Cloth> cl(new Cloth());
+  std::vector<int> bcv(np, 0);
+  if (bc) bcv.assign(bc, bc + np);
+  build_topology(cl->topo, np, X0, bcv.data(), nt, tri, nq, quad, prm->solver_kind == CS_SOLVER_ILU_PCG);
+  cl->prm = *prm;
+  cl->x.assign(X0, X0 + 3 * (size_t)np);
+  cl->v.assign(3 * (size_t)np, 0.0);
+  return cl;
+}
+
+size_t cloth_device_bytes(const ClothTopo& t) {
+  const size_t np = t.np, nt = t.nt, nq = t.nq, nb = t.nb, nn = t.nnode;
+  const size_t slots = t.slot_src.size() + t.grad_src.size() + 2 * (nb + 2 * np);
+  size_t b = 0;
+  b += np * (5 * 24 + 4 * 2);                  // X0 x v x1 v0, bc vinst
+  b += nt * (16 + 81 * 8 + 9 * 8);             // tri tinst, element blocks and gradients
+  b += nq * (20 + 4 * 8 + 8 + 12 * 8);         // quad qinst, bending factors, gradients
+  b += (np + 1) * 8 + nb * 8;                  // row_ptr dia_split, col_idx blk_row
+  b += slots * 4;                              // slot and gradient source lists
+  b += (nb + np) * 9 * 8 * 2;                  // matrix and ILU factor values
+  b += np * 5 * 24;                            // b r p z dx
+  b += (t.lev_rows.size() + t.blev_rows.size() + t.lev_ptr.size() + t.blev_ptr.size() + t.fac_ops.size() +
+        np + 1) * 4 + np * 4;                  // ILU schedule, singular flags
+  b += nn * (7 * 4 + 4 + 48 + 24 + 4) + nt * 4; // BVH arrays, counters, boxes (FP64 + FP32), tri_leaf
+  b += np * (24 + 3 * 4) + t.edge_uv.size() * 4;  // vertex boxes (FP32), dirty / zone flags, edges
+  const size_t sell = ((np + 31) / 32) * 32 * 16;  // SELL entries, padded to the slice width
+  b += sell * (36 + 4) + (nb + np) * 8;        // FP32 values, columns, SELL positions
+  b += np * (36 + 5 * 12);                     // FP32 diagonal inverse and vectors
+  b += (16 * nt + 4096) * 8 + (4 * nt + 4096) * 120;  // pair and candidate buffers
+  b += np * (2 * 4 + 2 * 8 + 72);              // vertex marks, zone keys and sums
+  return b + (1 << 16);
 }
 
 Cloth& cloth_at(cs_ctx* c, int id) {
@@ -819,7 +850,10 @@ void ensure(cs_ctx* c) {
   CK(cudaSetDevice(c->device));
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace cs
+
+using namespace cs::host;
 
 extern "C" {
 
@@ -838,6 +872,8 @@ int cs_create(int device, int precision, cs_ctx** out) {
     return CS_ERR_CUDA;
   }
   c->launches0 = g_launches;
+  if (const char* e = std::getenv("CLOTHGPU_MX_PERSISTENT")) c->mx_persistent = std::atoi(e) != 0;
+  if (const char* e = std::getenv("CLOTHGPU_MX_BLOCKS_PER_SM")) c->mx_blocks_per_sm = std::atoi(e);
   *out = c;
   return CS_OK;
 }
@@ -870,18 +906,12 @@ int cs_synchronize(cs_ctx* c) {
 int cs_add_cloth(cs_ctx* c, int np, const double* X0, const int* bc, int nt, const int* tri, int nq,
                  const int* quad, const cs_params* prm, int* id_out) {
   return guarded(c, [&] {
-    if (np <= 0 || nt <= 0 || nq < 0 || !X0 || !tri || (nq > 0 && !quad) || !prm)
-      throw ArgError("cs_add_cloth: bad sizes or null arrays");
-    if (prm->solver_kind != CS_SOLVER_ILU_PCG && prm->solver_kind != CS_SOLVER_CG)
-      throw ArgError("cs_add_cloth: unknown solver");
-    if (prm->obstacle_kind < 0 || prm->obstacle_kind > 3) throw ArgError("cs_add_cloth: unknown obstacle");
-    std::unique_ptr<Cloth> cl(new Cloth());
-    std::vector<int> bcv(np, 0);
-    if (bc) bcv.assign(bc, bc + np);
-    build_topology(cl->topo, np, X0, bcv.data(), nt, tri, nq, quad, prm->solver_kind == CS_SOLVER_ILU_PCG);
-    cl->prm = *prm;
-    cl->x.assign(X0, X0 + 3 * (size_t)np);
-    cl->v.assign(3 * (size_t)np, 0.0);
+    std::unique_ptr<Cloth> cl;
+    try {
+      cl = make_cloth(np, X0, bc, nt, tri, nq, quad, prm);
+    } catch (const ArgError& e) {
+      throw ArgError(std::string("cs_add_cloth: ") + e.what());
+    }
     save_states(c);
     cl->id = c->next_id++;
     c->order.push_back(cl->id);
@@ -1421,6 +1451,7 @@ int cs_profile_bytes(cs_ctx* c, long long* spmv32, long long* spmv64) {
     prof_count("fp64_ee_prx", (long long)h[3]);
     prof_count("fp64_fv_ccd", (long long)h[4]);
     prof_count("fp64_ee_ccd", (long long)h[5]);
+    prof_count("persist_bytes", (long long)h[6]);
   });
 }
 

@@ -50,6 +50,8 @@ struct InstState {
   int total_iters;   // inner iterations summed over refinement cycles
   int cycles;        // refinement cycles
   double red[3];     // per-cloth totals of the slice partials: p.q, r.z, r.r
+  // persistent inner solve: r.z of the iterations by parity
+  double rzh[2];
 };
 
 struct Arena {
@@ -115,6 +117,12 @@ struct Arena {
                                             // tests reaching FP64: FV prx, EE prx, FV ccd, EE ccd
   int count_bytes = 0;
   int mixed = 0;                    // mixed-precision arrays present
+  // persistent inner solve: a second direction buffer (the direction is built on
+  // the fly from the previous one), per-slice algorithmic bytes of one iteration,
+  // and the grid barrier state
+  long long* slice_pbytes = nullptr;
+  float* p32b = nullptr;
+  unsigned int* grid_bar = nullptr; // [0] arrivals, [1] generation, [2] gave up, [3] cloths still iterating
 };
 
 // scratch for the contact pipeline (grown on demand)

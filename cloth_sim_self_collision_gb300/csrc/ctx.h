@@ -1,0 +1,133 @@
+// ctx.h -- host-side internals of a context (include/clothgpu.h's cs_ctx):
+// the cloths it holds, the device arena they are packed into, and the frame
+// orchestration that the C ABI (api.cu) and the serving loop (serve.cu) share.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/clothgpu.h"
+#include "kernels.h"
+#include "topology.h"
+
+namespace cs {
+namespace host {
+
+struct ArgError : std::runtime_error {
+  explicit ArgError(const std::string& s) : std::runtime_error(s) {}
+};
+struct CapacityError : std::runtime_error {
+  explicit CapacityError(const std::string& s) : std::runtime_error(s) {}
+};
+
+#define CK(expr)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (expr);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      throw CudaError(std::string(#expr) + ": " + cudaGetErrorString(e_) + " (" __FILE__ ":" +   \
+                      std::to_string(__LINE__) + ")");                                            \
+  } while (0)
+
+struct Cloth {
+  int id = 0;
+  ClothTopo topo;
+  cs_params prm{};
+  std::vector<double> x, v;  // host copy, authoritative only while the arena is rebuilt
+  cs_stats stats{};
+};
+
+// device allocation with ownership in the context
+struct DevMem {
+  std::vector<void*> ptrs;
+  template <typename T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) throw CudaError(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    ptrs.push_back(p);
+    return (T*)p;
+  }
+  template <typename T>
+  T* upload(const std::vector<T>& h, cudaStream_t s) {
+    T* d = alloc<T>(h.size());
+    if (!h.empty()) CK(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+// one packing of cloths into a device arena, with its host mirrors
+struct ArenaSet {
+  Arena A;
+  ContactBufs C;
+  DevMem mem, cmem;
+  std::vector<int> order;  // arena slot -> cloth id
+  std::vector<int> voff, toff, qoff, boff, noff, solver;
+  int* d_list = nullptr;
+  std::vector<InstState> hst;
+  ~ArenaSet() {
+    mem.release();
+    cmem.release();
+  }
+};
+
+}  // namespace host
+}  // namespace cs
+
+struct cs_ctx {
+  int device = 0;
+  int precision = CS_PREC_FP64;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::map<int, std::unique_ptr<cs::host::Cloth>> cloths;
+  std::vector<int> order;  // arena slot -> cloth id
+  int next_id = 0;
+  bool dirty = true;
+  cs::Arena A;
+  cs::ContactBufs C;
+  cs::host::DevMem mem, cmem;  // arena / contact buffers
+  // host mirrors of arena offsets
+  std::vector<int> voff, toff, boff, noff, qoff;
+  std::vector<int> solver;  // per slot
+  int* d_list = nullptr;    // scratch list of cloth slots
+  int token = 0;
+  int last_ncand = 0;  // candidates of the last detection (kept in C.cand)
+  int last_nce = 0;    // contacts of the last detection (in C.ce)
+  std::vector<cs::InstState> hst;
+  long long launches0 = 0;
+  // mixed precision: whole inner solves as one cooperative launch (else one
+  // launch per kernel and iteration), and its blocks per SM (0: occupancy limit)
+  bool mx_persistent = true;
+  int mx_blocks_per_sm = 0;
+};
+
+namespace cs {
+namespace host {
+
+// Validates the arguments and builds the cloth's host topology (adjacency,
+// BVH, matrix pattern, ILU schedule): the expensive host part of admitting a
+// cloth.  Touches no context, so any thread may call it.
+std::unique_ptr<Cloth> make_cloth(int np, const double* X0, const int* bc, int nt, const int* tri, int nq,
+                                  const int* quad, const cs_params* prm);
+// device bytes a cloth adds to an arena (buffers sized by its vertices,
+// triangles, stencils, blocks and BVH nodes), used for admission by memory
+size_t cloth_device_bytes(const ClothTopo& t);
+// Packs cloths into a fresh arena on stream s; reads only the cloths.
+void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t s);
+// Makes o the context's arena; o receives the previous arena's buffers.
+void install(cs_ctx* c, ArenaSet& o);
+// one frame (StepTime) for the arena slots with act[slot] != 0
+void frame(cs_ctx* c, const std::vector<int>& act);
+// maps an exception from the host layer to a CS_* status and records its message
+int status_of(const std::exception& e, std::string* msg);
+
+}  // namespace host
+}  // namespace cs

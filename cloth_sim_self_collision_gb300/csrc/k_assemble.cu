@@ -13,7 +13,7 @@
 
 namespace cs {
 
-long long g_launches = 0;
+std::atomic<long long> g_launches{0};
 
 namespace {
 

@@ -131,6 +131,9 @@ __global__ void k_vertex_bounds(Arena A, int ccd, const double* xs, const double
   }
 }
 
+// Reserves one slot per active lane with one atomic per warp.  The counter may
+// pass INT_MAX (and wrap) when a buffer overflows badly: callers compare the
+// slot as unsigned against their capacity, so a wrapped slot is never written.
 __device__ __forceinline__ int warp_append(int* counter) {
   const unsigned m = __activemask();
   const int lane = threadIdx.x & 31;
@@ -161,7 +164,7 @@ __global__ void k_traverse(Arena A, ContactBufs C) {
     }
     if (A.node[3 * n + 2] == -1) {
       const int slot = warp_append(&C.counters[0]);
-      if (slot < C.pair_cap)
+      if ((unsigned)slot < (unsigned)C.pair_cap)
         C.pairs[slot] = make_int2(la, n);
       else
         C.counters[3] = 1;
@@ -195,7 +198,7 @@ __global__ void k_traverse_dirty(Arena A, ContactBufs C) {
       const bool other_dirty = A.tdirty[A.node[3 * n + 1]] != 0;
       if (n != la && (!other_dirty || oa < ob)) {
         const int slot = warp_append(&C.counters[0]);
-        if (slot < C.pair_cap)
+        if ((unsigned)slot < (unsigned)C.pair_cap)
           C.pairs[slot] = (oa < ob) ? make_int2(la, n) : make_int2(n, la);
         else
           C.counters[3] = 1;
@@ -262,7 +265,7 @@ __device__ __forceinline__ void canonical(int fv, int j0, int j1, int j2, int j3
 __device__ __forceinline__ void emit(const ContactBufs& C, int fv, int j0, int j1, int j2, int j3, int na, int nb,
                                      int test) {
   const int slot = warp_append(&C.counters[1]);
-  if (slot >= C.cand_cap) {
+  if ((unsigned)slot >= (unsigned)C.cand_cap) {
     C.counters[3] = 1;
     return;
   }

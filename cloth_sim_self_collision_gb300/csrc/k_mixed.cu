@@ -9,6 +9,8 @@
 // dx in FP64 and recomputes r = b - A dx with the FP64 matrix.  Cycles stop at
 // the reference's criterion |r|^2 / |b|^2 < tol^2 (Solve_CG / Solve_PCG,
 // matrix_square_sparse.cpp:338-406, ilu_sparse.cpp:628-709).
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace cs {
@@ -215,6 +217,215 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
   }
 }
 
+// ---- persistent inner solve ---------------------------------------------------------
+// One cooperative launch runs every inner CG iteration of a refinement cycle for
+// all cloths.  Each block owns a contiguous range of slices (and so touches one
+// or a few cloths); its warps take the range's slices in turn.  Per iteration,
+// two phases separated by grid barriers:
+//   A: from the r.z and r.r slice partials of the previous phase B, every block
+//      touching a cloth computes the cloth's totals itself (a fixed-order block
+//      sum over all its slices) and decides convergence (|r|^2 <= eta^2 |r0|^2,
+//      or the cap) or beta; then p = z + beta p_prev is built on the fly (for
+//      the rows a slice reads and for its own rows, which it stores),
+//      q = A32 p, and the slice partials of p.q are written.
+//   B: from the p.q partials, alpha = r.z / p.q per cloth (again computed by
+//      every block that needs it), then d += alpha p, r -= alpha q,
+//      z = D^-1 r, and the slice partials of r.z and r.r.
+// The block holding a cloth's first slice records its convergence and
+// decrements the count of cloths still iterating; every block reads that count
+// right after the barrier that follows phase A (nothing changes it before the
+// next phase A), so all blocks leave the loop together.  The direction buffers
+// alternate between iterations.  Totals are the same fixed-order sums in every
+// block: results depend neither on the launch shape nor on the other cloths.
+constexpr int kPersistThreads = 256;
+constexpr int kPersistWarps = kPersistThreads / 32;
+constexpr unsigned kSpinLimit = 1u << 22;  // ~1 s of polling at the least
+
+// Grid-wide barrier on A.grid_bar with a bounded wait.  Returns false when the
+// wait ran out here or in another block (the flag A.grid_bar[2] is then set and
+// every block leaves the kernel at its next barrier).
+__device__ bool grid_sync(const Arena& A) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* bar = A.grid_bar;
+    __threadfence();
+    const unsigned gen = bar[1];
+    if (atomicAdd(&A.grid_bar[0], 1u) == gridDim.x - 1) {
+      atomicExch(&A.grid_bar[0], 0u);
+      __threadfence();
+      atomicAdd(&A.grid_bar[1], 1u);
+    } else {
+      unsigned n = 0;
+      while (bar[1] == gen && bar[2] == 0u) {
+        if (++n > kSpinLimit) {
+          atomicExch(&A.grid_bar[2], 1u);
+          break;
+        }
+        __nanosleep(256);
+      }
+    }
+    __threadfence();
+    s_ok = bar[2] == 0u;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Totals over the slices of cloth inst of nf partial fields starting at f0, as
+// fixed-order block sums (every thread gets them in tot[]).
+__device__ void cloth_totals(const Arena& A, int inst, int f0, int nf, double* sh, double* tot) {
+  const int lo = A.slice_lo[inst], hi = A.slice_hi[inst];
+  for (int f = 0; f < nf; f++) {
+    double v = 0.0;
+    for (int k = lo + threadIdx.x; k < hi; k += kPersistThreads) v += __ldcg(&A.part32[3 * k + f0 + f]);
+    v = warp_sum_d(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < kPersistWarps; w++) t += sh[w];
+    tot[f] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float eta, int cap) {
+  __shared__ double sh[kPersistWarps];
+  __shared__ int s_left;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this block's slices [s0, s1)
+  const long long S = A.nslice;
+  const int s0 = (int)(S * blockIdx.x / gridDim.x), s1 = (int)(S * (blockIdx.x + 1) / gridDim.x);
+  const int c0 = s0 < s1 ? A.slice_inst[s0] : 0, c1 = s0 < s1 ? A.slice_inst[s1 - 1] : -1;
+  for (int it = 1; it <= cap + 1; it++) {
+    const float* Pold = (it & 1) ? A.p32 : A.p32b;
+    float* Pnew = (it & 1) ? A.p32b : A.p32;
+    // ---- phase A: convergence, direction, SpMV
+    for (int inst = c0; inst <= c1; inst++) {
+      if (!A.active[inst]) continue;
+      InstState& St = A.st[inst];
+      if (St.done || St.idone) continue;
+      const bool owner = s0 <= A.slice_lo[inst] && A.slice_lo[inst] < s1;
+      float beta = 0.f;
+      if (it > 1) {
+        double tot[2];
+        cloth_totals(A, inst, 1, 2, sh, tot);
+        if (tot[1] <= (double)eta * (double)eta * St.rr_in0 || it - 1 >= cap) {
+          if (owner && threadIdx.x == 0) {
+            St.idone = 1;
+            St.inner_iters = it - 1;
+            St.red[1] = tot[0];
+            St.red[2] = tot[1];
+            atomicSub(&A.grid_bar[3], 1u);
+          }
+          continue;
+        }
+        beta = (float)(tot[0] / St.rzh[(it - 1) & 1]);
+        if (owner && threadIdx.x == 0) {
+          St.rzh[it & 1] = tot[0];
+          St.inner_iters = it - 1;
+        }
+      }
+      const int lo = max(s0, A.slice_lo[inst]), hi = min(s1, A.slice_hi[inst]);
+      for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
+        const int row = A.slice_row0[sl] + lane;
+        const int w = A.slice_w[sl];
+        const float* V = A.val32 + A.slice_voff[sl] + lane;
+        const int* Cc = A.col32 + A.slice_coff[sl] + lane;
+        float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll 2
+        for (int j = 0; j < w; j++) {
+          const int col = Cc[32 * j];
+          const float x0 = fmaf(beta, Pold[3 * col + 0], A.z32[3 * col + 0]);
+          const float x1 = fmaf(beta, Pold[3 * col + 1], A.z32[3 * col + 1]);
+          const float x2 = fmaf(beta, Pold[3 * col + 2], A.z32[3 * col + 2]);
+          const float* v = V + 288 * j;
+          y0 = fmaf(v[0], x0, fmaf(v[32], x1, fmaf(v[64], x2, y0)));
+          y1 = fmaf(v[96], x0, fmaf(v[128], x1, fmaf(v[160], x2, y1)));
+          y2 = fmaf(v[192], x0, fmaf(v[224], x1, fmaf(v[256], x2, y2)));
+        }
+        float pq = 0.f;
+        if (row < A.voff[inst + 1]) {
+          float p[3];
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            p[k] = fmaf(beta, Pold[3 * row + k], A.z32[3 * row + k]);
+            Pnew[3 * row + k] = p[k];
+          }
+          A.q32[3 * row + 0] = y0;
+          A.q32[3 * row + 1] = y1;
+          A.q32[3 * row + 2] = y2;
+          pq = p[0] * y0 + p[1] * y1 + p[2] * y2;
+        }
+        pq = warp_sum_f(pq);
+        if (lane == 0) {
+          A.part32[3 * sl + 0] = pq;
+          if (A.count_bytes) atomicAdd(&A.bytes_acc[6], (unsigned long long)A.slice_pbytes[sl]);
+        }
+      }
+    }
+    if (!grid_sync(A)) return;
+    if (threadIdx.x == 0) s_left = ((volatile unsigned*)A.grid_bar)[3] != 0u;
+    __syncthreads();
+    if (!s_left) break;
+    // ---- phase B: step length and update
+    for (int inst = c0; inst <= c1; inst++) {
+      if (!A.active[inst]) continue;
+      InstState& St = A.st[inst];
+      if (St.done || St.idone) continue;
+      double tot[1];
+      cloth_totals(A, inst, 0, 1, sh, tot);
+      const float alpha = (float)(St.rzh[it & 1] / tot[0]);
+      const int lo = max(s0, A.slice_lo[inst]), hi = min(s1, A.slice_hi[inst]);
+      for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
+        const int row = A.slice_row0[sl] + lane;
+        float rz = 0.f, rr = 0.f;
+        if (row < A.voff[inst + 1]) {
+          float r[3], z[3];
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            const int i = 3 * row + k;
+            A.d32[i] = fmaf(alpha, Pnew[i], A.d32[i]);
+            r[k] = fmaf(-alpha, A.q32[i], A.r32[i]);
+            A.r32[i] = r[k];
+          }
+          apply_dinv(A.dinv32 + 9 * (size_t)row, r, z);
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            A.z32[3 * row + k] = z[k];
+            rz += r[k] * z[k];
+            rr += r[k] * r[k];
+          }
+        }
+        rz = warp_sum_f(rz);
+        rr = warp_sum_f(rr);
+        if (lane == 0) {
+          A.part32[3 * sl + 1] = rz;
+          A.part32[3 * sl + 2] = rr;
+        }
+      }
+    }
+    if (!grid_sync(A)) return;
+  }
+}
+
+// inner-solve start for the persistent kernel: totals of r.z and r.r per cloth
+// and the count of cloths that iterate
+__global__ void k_mx_pstart(Arena A) {
+  const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (inst >= A.ni || !A.active[inst] || A.st[inst].done) return;
+  const double rz = cloth_total(A, inst, 1), rr = cloth_total(A, inst, 2);
+  if ((threadIdx.x & 31) == 0) {
+    InstState& S = A.st[inst];
+    S.rzh[1] = rz;  // iteration 1 reads parity 1
+    S.rr_in0 = rr;
+    S.idone = (rr <= 0.0) ? 1 : 0;
+    S.inner_iters = 0;
+    if (!S.idone) atomicAdd(&A.grid_bar[3], 1u);
+  }
+}
+
 // ---- FP64 outer refinement --------------------------------------------------------
 __device__ __forceinline__ int chunk_row(const Arena& A, int c, int inst) {
   return A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk + threadIdx.x;
@@ -380,6 +591,27 @@ void launch_mx_inner_iteration(const Arena& A, int it, float eta, int cap, cudaS
   k_mx_direction<<<blocks, kSliceThreads, 0, s>>>(A, it, eta, cap);
   prof_end(PK_MX_DIRECTION, s);
   g_launches += 3;
+}
+
+void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, cudaStream_t s) {
+  launch_check(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s), "cudaMemsetAsync");
+  const int blocks = (A.nslice * 32 + kSliceThreads - 1) / kSliceThreads;
+  k_mx_inner_init<<<blocks, kSliceThreads, 0, s>>>(A);
+  k_mx_pstart<<<(A.ni * 32 + 127) / 128, 128, 0, s>>>(A);
+  g_launches += 2;
+  int dev = 0, sms = 0, occ = 0;
+  launch_check(cudaGetDevice(&dev), "cudaGetDevice");
+  launch_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+  launch_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mx_persist, kPersistThreads, 0),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+  if (blocks_per_sm > 0) occ = std::min(occ, blocks_per_sm);
+  // at least one slice per warp
+  const int grid = std::max(1, std::min((A.nslice + kPersistWarps - 1) / kPersistWarps, sms * std::max(occ, 1)));
+  void* args[] = {(void*)&A, (void*)&eta, (void*)&cap};
+  prof_begin(PK_MX_PERSIST, s);
+  launch_check(cudaLaunchCooperativeKernel((const void*)k_mx_persist, dim3(grid), dim3(kPersistThreads), args, 0, s), "cudaLaunchCooperativeKernel");
+  prof_end(PK_MX_PERSIST, s);
+  g_launches += 1;
 }
 
 void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s) {

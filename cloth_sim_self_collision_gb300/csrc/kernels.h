@@ -1,13 +1,25 @@
 // kernels.h -- host launchers of the device kernels (one translation unit each
 // for assembly, solvers and collision).
 #pragma once
+#include <atomic>
+#include <stdexcept>
+#include <string>
+
 #include "arena.h"
 #include "prof.h"
 
 namespace cs {
 
+// a failed CUDA call (the C ABI reports it as CS_ERR_CUDA, or CS_ERR_OOM)
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+inline void launch_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
 // launches issued by this process (all contexts), for launch accounting
-extern long long g_launches;
+extern std::atomic<long long> g_launches;
 
 // --- assembly (k_assemble.cu) ---------------------------------------------
 void launch_quad_factors(const Arena& A, cudaStream_t s);
@@ -42,6 +54,9 @@ void launch_mx_inner_init(const Arena& A, cudaStream_t s);
 // dx = dt v and r = b - A dx (FP64) for the active, unconverged cloths
 void launch_mx_warm_start(const Arena& A, cudaStream_t s);
 void launch_mx_inner_iteration(const Arena& A, int it, float eta, int cap, cudaStream_t s);
+// the whole inner FP32 CG of one refinement cycle (up to cap iterations) in one
+// cooperative launch; blocks_per_sm <= 0 picks the occupancy limit
+void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, cudaStream_t s);
 void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s);
 
 // --- collision (k_collide.cu) ------------------------------------------------

@@ -9,7 +9,8 @@ namespace cs {
 const char* const kProfNames[PK_COUNT] = {"tri_elements", "slot_reduce", "rhs",     "ilu_factor",
                                           "pcg",          "cg_spmv",     "cg_update", "cg_direction",
                                           "refit",        "traverse",    "narrow",    "impulse",
-                                          "mx_spmv",      "mx_update",   "mx_direction", "mx_residual"};
+                                          "mx_spmv",      "mx_update",   "mx_direction", "mx_residual",
+                                          "mx_persist"};
 
 namespace {
 struct Pending {
@@ -22,9 +23,11 @@ std::vector<cudaEvent_t> g_free;
 cudaEvent_t g_open[PK_COUNT];
 double g_ms[PK_COUNT];
 long long g_n[PK_COUNT];
-const char* const kCountNames[8] = {"pairs", "candidates", "contacts", "detections",
-                                    "fp64_fv_prx", "fp64_ee_prx", "fp64_fv_ccd", "fp64_ee_ccd"};
-long long g_counts[8];
+constexpr int kNumCounts = 9;
+const char* const kCountNames[kNumCounts] = {"pairs",       "candidates",  "contacts",    "detections",
+                                             "fp64_fv_prx", "fp64_ee_prx", "fp64_fv_ccd", "fp64_ee_ccd",
+                                             "persist_bytes"};
+long long g_counts[kNumCounts];
 
 cudaEvent_t get_event() {
   if (!g_free.empty()) {
@@ -77,13 +80,13 @@ void prof_reset() {
 
 void prof_count(const char* name, long long n) {
   if (!g_on) return;
-  for (int k = 0; k < 8; k++)
+  for (int k = 0; k < kNumCounts; k++)
     if (std::strcmp(name, kCountNames[k]) == 0) g_counts[k] += n;
 }
 
 bool prof_read(const char* name, double* total_ms, long long* launches) {
   prof_collect();
-  for (int k = 0; k < 8; k++)
+  for (int k = 0; k < kNumCounts; k++)
     if (std::strcmp(name, kCountNames[k]) == 0) {
       if (total_ms) *total_ms = 0;
       if (launches) *launches = g_counts[k];

@@ -22,6 +22,7 @@ enum ProfKernel {
   PK_MX_UPDATE,
   PK_MX_DIRECTION,
   PK_MX_RESIDUAL,
+  PK_MX_PERSIST,
   PK_COUNT
 };
 

@@ -211,6 +211,66 @@ int cs_get_states(cs_ctx *ctx, double *x, double *v);
 /* Total vertices of the context (length of the state arrays / 3). */
 long long cs_num_vertices(const cs_ctx *ctx);
 
+/* ---- serving: continuous batching of scenes on one GPU ---------------------------- */
+/* No counterpart in the reference (its driver steps one cloth in a GLUT loop).  A
+ * server owns one context whose arena holds every admitted scene; a worker thread
+ * advances all unfinished scenes together, one StepTime frame per loop, while scenes
+ * that arrive are packed into the next arena by a builder thread and swapped in at a
+ * frame boundary (their positions and velocities stay on the device).  Admission is
+ * first come, first served by estimated device bytes: the arena being stepped plus
+ * the one being packed stay within hbm_budget_bytes.  A scene computes the same
+ * frames alone and in a mix (every reduction, sort and schedule is per cloth). */
+typedef struct cs_server cs_server;
+
+typedef struct cs_server_config {
+  int device;               /* CUDA device ordinal                                   */
+  int precision;            /* CS_PREC_FP64 or CS_PREC_MIXED                         */
+  double hbm_budget_bytes;  /* admission limit on estimated device bytes             */
+  int max_cloths;           /* limit on scenes per arena, 0 for none                 */
+} cs_server_config;
+
+typedef struct cs_request_info {
+  int np, nsteps, steps_done;
+  int status;               /* CS_OK, or the error that ended the request            */
+  double t_submit, t_admit, t_first_frame, t_done;  /* seconds since cs_server_create */
+  double step_ms_p50, step_ms_p99;                   /* frames the scene took part in */
+} cs_request_info;
+
+typedef struct cs_server_stats {
+  long long frames, vertex_steps;
+  int submitted, finished, queued, resident, rebuilds;
+  double elapsed_s, busy_s;                  /* since creation; inside frames           */
+  double step_ms_p50, step_ms_p99, step_ms_max;  /* over (scene, frame) samples        */
+  double admit_ms_p50, admit_ms_p99;         /* submission to first frame               */
+  double build_ms_total;                     /* packing new arenas, overlapped with frames */
+  double install_ms_total;                   /* frame-boundary swaps                    */
+  double arena_bytes, peak_bytes;            /* estimated device bytes                  */
+} cs_server_stats;
+
+int cs_server_create(const cs_server_config *cfg, cs_server **out);
+/* Queues a scene (mesh as in cs_add_cloth; x, v: initial state, null for X0 and
+ * rest) for nsteps frames.  Builds its host topology on the calling thread and
+ * returns at once; CS_ERR_CAPACITY if the scene alone exceeds the budget.
+ * Thread-safe. */
+int cs_server_submit(cs_server *srv, int np, const double *X0, const int *bc, int nt, const int *tri,
+                     int nq, const int *quad, const double *x, const double *v, const cs_params *prm,
+                     int nsteps, int *req);
+/* Waits (timeout_s < 0: without limit; CS_ERR_TIMEOUT when it runs out) until the
+ * request has run its frames, then copies its final state (x, v may be null).
+ * Returns the request's status. */
+int cs_server_wait(cs_server *srv, int req, double timeout_s, double *x, double *v, cs_request_info *info);
+/* Frees the host copy of a finished request's final state. */
+int cs_server_release(cs_server *srv, int req);
+/* Waits until every submitted request has finished. */
+int cs_server_drain(cs_server *srv, double timeout_s);
+int cs_server_get_stats(cs_server *srv, cs_server_stats *st);
+const char *cs_server_last_error(cs_server *srv);
+/* Stops the worker after its current frame; unfinished requests are dropped. */
+void cs_server_destroy(cs_server *srv);
+/* The admission estimate of a scene's device bytes (0 for invalid arguments). */
+size_t cs_scene_device_bytes(int np, const double *X0, int nt, const int *tri, int nq, const int *quad,
+                             const cs_params *prm);
+
 /* ---- a solve that allocates nothing ---------------------------------------------- */
 /* Maximum block rows (vertices) accepted by cs_solve_cg_noalloc. */
 #define CS_NOALLOC_MAX_VERTICES 16384
