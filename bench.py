@@ -200,6 +200,81 @@ def plain_one_per_launch(cloths, device, frames: int, budget_s: float = 8.0) -> 
                       f"inner products), frames 2..{frames + 1}"}
 
 
+def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, plain_frames: int = 10,
+            plain_scenes: int = 6) -> dict:
+    """The serving workload: scenes of log-uniform size (1e2..1e5 vertices) arriving
+    as a Poisson process, each run for `steps` frames by the native server (one
+    arena, continuous batching, admission by a 150 GB device-byte budget).
+    Throughput counts the vertex-steps of scenes that finished; scenes whose frames
+    blew up (CS_ERR_DIVERGED) are counted apart.  The plain FP64 path runs a
+    sample of the same scenes one per context, for `plain_frames` frames each."""
+    import torch
+
+    from cloth_sim_self_collision_gb300 import _native as N
+    from cloth_sim_self_collision_gb300 import scene
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    from cloth_sim_self_collision_gb300.serve import Server
+    cl = scene.config_serving(scenes)
+    arr = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, scenes))
+    infos, diverged = [], 0
+    with Server(device, "mixed", 150e9) as srv:
+        reqs = []
+        t0 = time.perf_counter()
+        for c, a in zip(cl, arr):
+            wait = a - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            reqs.append(srv.submit(c, steps))
+        for c, r in zip(cl, reqs):
+            try:
+                infos.append((c, srv.wait(r, timeout=900.0)[2]))
+            except N.CsError as e:
+                if e.code != N.CS_ERR_DIVERGED:
+                    raise
+                diverged += 1
+        st = srv.stats()
+    done = [(c, i) for c, i in infos]
+    span = max(i["t_done"] for _, i in done) - min(i["t_submit"] for _, i in done) if done else float("nan")
+    vsteps = sum(c.np * steps for c, _ in done)
+    # the plain FP64 path, one scene per context, on a sample of the same scenes
+    ctx = ClothContext(device, "fp64")
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+    pv, pms, used = 0, 0.0, 0
+    for c in cl[:plain_scenes]:
+        cid = ctx.add_cloth(c)
+        ctx.step(1)
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.step(plain_frames)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if not ctx.stats(cid)["diverged"]:
+            pms += e0.elapsed_time(e1)
+            pv += c.np * plain_frames
+            used += 1
+        ctx.remove_cloth(cid)
+    ctx.close()
+    out = {
+        "workload": f"{scenes} scenes, vertex count log-uniform 1e2..1e5 (square grids), Poisson arrivals at "
+                    f"{rate}/s, {steps} frames each, 150 GB admission budget, mixed precision",
+        "vertex_steps_per_s": vsteps / span if done else None, "completed": len(done), "diverged": diverged,
+        "p50_step_ms": st["step_ms_p50"], "p99_step_ms": st["step_ms_p99"], "max_step_ms": st["step_ms_max"],
+        "admit_ms_p50": st["admit_ms_p50"], "admit_ms_p99": st["admit_ms_p99"],
+        "p50_request_s": float(np.percentile([i["t_done"] - i["t_submit"] for _, i in done], 50)) if done else None,
+        "p99_request_s": float(np.percentile([i["t_done"] - i["t_submit"] for _, i in done], 99)) if done else None,
+        "frames": st["frames"], "arena_swaps": st["rebuilds"], "build_ms_total": st["build_ms_total"],
+        "swap_ms_total": st["install_ms_total"], "peak_bytes": st["peak_bytes"],
+        "plain_gpu_fp64_one_per_launch": {
+            "value": pv / (pms / 1e3) if pms > 0 else None, "unit": UNIT,
+            "sample": f"first {plain_scenes} scenes ({used} that did not blow up), each alone in its own arena, "
+                      f"frames 2..{plain_frames + 1}"},
+    }
+    if out["vertex_steps_per_s"] and out["plain_gpu_fp64_one_per_launch"]["value"]:
+        out["vs_plain_gpu"] = out["vertex_steps_per_s"] / out["plain_gpu_fp64_one_per_launch"]["value"]
+    return out
+
+
 def native(args):
     import torch
 
@@ -316,6 +391,8 @@ def native(args):
     if plain is not None:
         line["plain_gpu_fp64_one_per_launch"] = plain
         line["vs_plain_gpu"] = head["value"] / plain["value"]
+    if not args.no_serve:
+        line["serving"] = serving(local, args.serve_scenes, args.serve_rate, args.serve_steps)
     if not args.no_cpu:
         line["cpu_baseline"] = run_cpu_baseline(cloths)
     print(json.dumps(line), flush=True)
@@ -407,6 +484,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the one-cloth-per-launch FP64 sample")
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
                     help="both: mixed is the headline, FP64 batched reported beside it")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving workload")
+    ap.add_argument("--serve-scenes", type=int, default=24)
+    ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, scenes per second")
+    ap.add_argument("--serve-steps", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
         raise SystemExit("need --steps >= 1 and --warmup >= 0")

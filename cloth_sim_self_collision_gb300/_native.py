@@ -21,6 +21,7 @@ CS_ERR_NO_DEVICE = 3
 CS_ERR_OOM = 4
 CS_ERR_CAPACITY = 5
 CS_ERR_TIMEOUT = 6
+CS_ERR_DIVERGED = 7
 
 CS_FLAG_EXACT_DOTS = 1
 
@@ -77,7 +78,7 @@ class CsStats(ctypes.Structure):
         ("solver_iterations", ctypes.c_int), ("n_prx", ctypes.c_int), ("n_ccd_passes", ctypes.c_int),
         ("n_ccd", ctypes.c_int * 5), ("n_riz_passes", ctypes.c_int), ("n_riz_last", ctypes.c_int),
         ("n_riz_total", ctypes.c_int), ("riz_nodes", ctypes.c_int), ("impulse_applied", ctypes.c_int),
-        ("ilu_singular", ctypes.c_int), ("solver_conv", ctypes.c_double),
+        ("ilu_singular", ctypes.c_int), ("solver_conv", ctypes.c_double), ("diverged", ctypes.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -104,7 +105,7 @@ class CsRequestInfo(ctypes.Structure):
 class CsServerStats(ctypes.Structure):
     _fields_ = [("frames", ctypes.c_longlong), ("vertex_steps", ctypes.c_longlong),
                 ("submitted", ctypes.c_int), ("finished", ctypes.c_int), ("queued", ctypes.c_int),
-                ("resident", ctypes.c_int), ("rebuilds", ctypes.c_int),
+                ("resident", ctypes.c_int), ("rebuilds", ctypes.c_int), ("diverged", ctypes.c_int),
                 ("elapsed_s", ctypes.c_double), ("busy_s", ctypes.c_double),
                 ("step_ms_p50", ctypes.c_double), ("step_ms_p99", ctypes.c_double),
                 ("step_ms_max", ctypes.c_double), ("admit_ms_p50", ctypes.c_double),

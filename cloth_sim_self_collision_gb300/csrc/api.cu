@@ -403,6 +403,8 @@ void install(cs_ctx* c, ArenaSet& o) {
   std::swap(c->solver, o.solver);
   std::swap(c->d_list, o.d_list);
   std::swap(c->hst, o.hst);
+  c->dead.assign(c->order.size(), 0);
+  for (size_t i = 0; i < c->order.size(); i++) c->dead[i] = c->cloths[c->order[i]]->stats.diverged;
   c->token = 0;
   c->last_ncand = 0;
   c->last_nce = 0;
@@ -434,8 +436,26 @@ void save_states(cs_ctx* c) {
   CK(cudaStreamSynchronize(c->stream));
 }
 
+// act without the cloths that blew up
+std::vector<int> live(const cs_ctx* c, const std::vector<int>& act) {
+  std::vector<int> a = act;
+  for (size_t i = 0; i < a.size() && i < c->dead.size(); i++)
+    if (c->dead[i]) a[i] = 0;
+  return a;
+}
+
 void set_active(cs_ctx* c, const std::vector<int>& act) {
-  CK(cudaMemcpyAsync(c->A.active, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, c->stream));
+  const std::vector<int> a = live(c, act);
+  CK(cudaMemcpyAsync(c->A.active, a.data(), sizeof(int) * a.size(), cudaMemcpyHostToDevice, c->stream));
+}
+
+// cloths whose broad phase flagged them as blown up stop here
+void note_divergence(cs_ctx* c) {
+  for (int i = 0; i < c->A.ni; i++)
+    if (c->hst[i].diverged && !c->dead[i]) {
+      c->dead[i] = 1;
+      c->cloths[c->order[i]]->stats.diverged = 1;
+    }
 }
 
 void pull_states(cs_ctx* c) {
@@ -586,6 +606,7 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
       int total = 0;
       CK(cudaMemcpyAsync(&total, c->C.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
       pull_states(c);
+      note_divergence(c);
       prof_count("pairs", cnt[0]);
       prof_count("candidates", ncand);
       prof_count("contacts", total);
@@ -631,6 +652,7 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
   int total = 0;
   CK(cudaMemcpyAsync(&total, c->C.counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
   pull_states(c);
+  note_divergence(c);
   prof_count("pairs", npairs);
   prof_count("candidates", ncand);
   prof_count("contacts", total);
@@ -643,6 +665,11 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
 void impulses(cs_ctx* c, int ccd, const double* xs, double* vs) {
   c->token++;
   launch_impulses(c->A, c->C, ccd, xs, vs, c->token, c->stream);
+}
+
+void drop_dead(const cs_ctx* c, std::vector<int>& phase, std::vector<int>& applied) {
+  for (size_t i = 0; i < phase.size(); i++)
+    if (c->dead[i]) phase[i] = applied[i] = 0;
 }
 
 // GetIntermidiateVelocityContactResolved (self_collision_cloth.cpp:355-456) for
@@ -664,6 +691,7 @@ std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
     }
   set_active(c, phase);
   detect(c, 0, A.x1, nullptr, -1.0);
+  drop_dead(c, phase, applied);
   for (int i = 0; i < ni; i++)
     if (act[i]) {
       c->cloths[c->order[i]]->stats.n_prx = c->hst[i].n_contacts;
@@ -677,6 +705,7 @@ std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
     set_active(c, phase);
     if (it > 0) launch_mark_dirty(A, c->C, c->last_nce, false, c->stream);
     detect(c, 1, A.x1, A.v, -1.0, it > 0);
+    drop_dead(c, phase, applied);
     for (int i = 0; i < ni; i++) {
       if (!phase[i]) continue;
       cs_stats& st = c->cloths[c->order[i]]->stats;
@@ -705,6 +734,7 @@ std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
       // CCD impulses) or, after a zone pass, at the zone vertices
       launch_mark_dirty(A, c->C, c->last_nce, it > 0, c->stream);
       detect(c, 1, A.x1, A.v, -1.0, true);
+      drop_dead(c, phase, applied);
       launch_riz_count(A, c->stream);
       pull_states(c);
       int nce = 0;
@@ -741,11 +771,13 @@ void update_velocity(cs_ctx* c, const std::vector<int>& act) {
 }
 
 // one frame for the cloths in act (StepTime, self_contact_sparse/main.cpp:213-263)
-void frame(cs_ctx* c, const std::vector<int>& act) {
+void frame(cs_ctx* c, const std::vector<int>& act_in) {
   const Arena& A = c->A;
+  const std::vector<int> act = live(c, act_in);
   CK(cudaMemcpyAsync(A.x1, A.x, sizeof(double) * 3 * (size_t)A.nv, cudaMemcpyDeviceToDevice, c->stream));
   implicit(c, act);
   pull_states(c);
+  note_divergence(c);
   for (int i = 0; i < A.ni; i++)
     if (act[i]) {
       cs_stats& st = c->cloths[c->order[i]]->stats;
@@ -753,7 +785,7 @@ void frame(cs_ctx* c, const std::vector<int>& act) {
       st.solver_conv = c->hst[i].solver_conv;
       st.ilu_singular = c->solver[i] == CS_SOLVER_ILU_PCG ? c->hst[i].ilu_singular : 0;
     }
-  std::vector<int> applied = resolve(c, act);
+  std::vector<int> applied = resolve(c, live(c, act));
   bool any = false;
   for (int i = 0; i < A.ni; i++) any |= applied[i] != 0;
   if (any) {

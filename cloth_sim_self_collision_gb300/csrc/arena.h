@@ -36,7 +36,7 @@ struct InstState {
   int solver_iterations;
   int ilu_singular;
   int done;          // solver converged
-  int pad;
+  int diverged;      // a triangle's broad phase exceeded kMaxPairsPerTriangle: the cloth stops
   double solver_conv;
   double sq[2];      // CG: r.r of the previous / current iteration (by parity)
   double inv0;

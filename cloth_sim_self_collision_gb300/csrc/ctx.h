@@ -107,6 +107,8 @@ struct cs_ctx {
   // launch per kernel and iteration), and its blocks per SM (0: occupancy limit)
   bool mx_persistent = true;
   int mx_blocks_per_sm = 0;
+  // per slot: the cloth blew up (CS_ERR_DIVERGED) and is no longer stepped
+  std::vector<int> dead;
 };
 
 namespace cs {

@@ -235,6 +235,8 @@ __global__ void k_update_velocity(Arena A) {
   }
 }
 
+// x += dx, v = dx / dt; a speed above kMaxSpeed (or not a number) marks the
+// cloth as blown up
 __global__ void k_finish_implicit(Arena A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * A.nv) return;
@@ -242,7 +244,9 @@ __global__ void k_finish_implicit(Arena A) {
   if (!A.active[inst]) return;
   const double d = A.dx[i];
   A.x[i] += d;
-  A.v[i] = d / A.prm[inst].dt;
+  const double v = d / A.prm[inst].dt;
+  A.v[i] = v;
+  if (!(fabs(v) <= kMaxSpeed)) A.st[inst].diverged = 1;
 }
 
 __global__ void k_reintegrate(Arena A) {

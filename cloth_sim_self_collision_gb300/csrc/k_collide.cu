@@ -145,17 +145,21 @@ __device__ __forceinline__ int warp_append(int* counter) {
 }
 
 // broad phase: leaf pairs with overlapping boxes (GetContactElement_* recursion,
-// bvh_aabb.cpp:441-557 / 797-923)
+// bvh_aabb.cpp:441-557 / 797-923).  A triangle that overlaps more than
+// kMaxPairsPerTriangle leaves to its right marks its cloth as blown up (the
+// reference would go on with a quadratic contact set); the cloth's pairs are
+// then dropped by the narrow phase and the host stops stepping it.
 __global__ void k_traverse(Arena A, ContactBufs C) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nt) return;
   const int inst = A.tinst[t];
-  if (!A.active[inst]) return;
+  if (!A.active[inst] || A.st[inst].diverged) return;
   const int la = A.tri_leaf[t];
   const int oa = A.leaf_lo[la];
   const Box ba = A.box[la];
   int k = A.preoff[inst];
   const int end = A.preoff[inst + 1];
+  int found = 0;
   while (k < end) {
     const int n = A.pre[k];
     if (A.leaf_hi[n] <= oa || !box_overlap(ba, A.box[n])) {
@@ -163,6 +167,10 @@ __global__ void k_traverse(Arena A, ContactBufs C) {
       continue;
     }
     if (A.node[3 * n + 2] == -1) {
+      if (++found > kMaxPairsPerTriangle) {
+        A.st[inst].diverged = 1;
+        return;
+      }
       const int slot = warp_append(&C.counters[0]);
       if ((unsigned)slot < (unsigned)C.pair_cap)
         C.pairs[slot] = make_int2(la, n);
@@ -177,16 +185,18 @@ __global__ void k_traverse(Arena A, ContactBufs C) {
 
 // every overlapping leaf pair with a dirty triangle, oriented by leaf order; a
 // pair of two dirty triangles is emitted by its left one
+// (overlaps on both sides are walked here: the blow-up limit is doubled)
 __global__ void k_traverse_dirty(Arena A, ContactBufs C) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nt || !A.tdirty[t]) return;
   const int inst = A.tinst[t];
-  if (!A.active[inst]) return;
+  if (!A.active[inst] || A.st[inst].diverged) return;
   const int la = A.tri_leaf[t];
   const int oa = A.leaf_lo[la];
   const Box ba = A.box[la];
   int k = A.preoff[inst];
   const int end = A.preoff[inst + 1];
+  int found = 0;
   while (k < end) {
     const int n = A.pre[k];
     if (!box_overlap(ba, A.box[n])) {
@@ -194,6 +204,10 @@ __global__ void k_traverse_dirty(Arena A, ContactBufs C) {
       continue;
     }
     if (A.node[3 * n + 2] == -1) {
+      if (++found > 2 * kMaxPairsPerTriangle) {
+        A.st[inst].diverged = 1;
+        return;
+      }
       const int ob = A.leaf_lo[n];
       const bool other_dirty = A.tdirty[A.node[3 * n + 1]] != 0;
       if (n != la && (!other_dirty || oa < ob)) {
@@ -302,6 +316,7 @@ __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, cons
   const int na = pr.x, nb = pr.y;
   const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
   const int inst = A.tinst[ta];
+  if (A.st[inst].diverged) return;
   const DevParams& P = A.prm[inst];
   const double delta = delta_override >= 0 ? delta_override : P.contact_clearance;
   if (test < 6) {

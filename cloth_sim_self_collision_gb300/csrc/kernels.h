@@ -10,6 +10,14 @@
 
 namespace cs {
 
+// Leaf pairs one triangle's broad-phase walk may emit before its cloth is taken
+// as blown up (normal frames stay far below: a few tens per triangle, a few
+// hundred in deep folds).
+constexpr int kMaxPairsPerTriangle = 512;
+// A velocity component above this (m/s) after the implicit step also marks the
+// cloth as blown up (no cloth frame of the reference's scenes comes near it).
+constexpr double kMaxSpeed = 1.0e3;
+
 // a failed CUDA call (the C ABI reports it as CS_ERR_CUDA, or CS_ERR_OOM)
 struct CudaError : std::runtime_error {
   explicit CudaError(const std::string& s) : std::runtime_error(s) {}

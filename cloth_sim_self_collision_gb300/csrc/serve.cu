@@ -88,7 +88,7 @@ struct cs_server {
   std::string err;
   Clock::time_point t0;
   long long frames = 0, vsteps = 0;
-  int rebuilds = 0, submitted = 0, finished = 0;
+  int rebuilds = 0, submitted = 0, finished = 0, diverged = 0;
   double busy_s = 0, build_ms = 0, install_ms = 0;
   std::vector<float> samples, admit_ms;
 };
@@ -283,12 +283,14 @@ void worker_main(cs_server* S) {
       frame(S->ctx, act);
       CK(cudaStreamSynchronize(S->ctx->stream));
       const float ms = (float)(1e3 * seconds_since(t));
-      // final states of the scenes that finished with this frame
+      // final states of the scenes that finished with this frame (a scene that
+      // blew up ends here with CS_ERR_DIVERGED)
       std::vector<int> fin;
       {
         std::lock_guard<std::mutex> lk(S->mu);
         for (size_t i = 0; i < act.size(); i++)
-          if (act[i] && S->reqs[S->slots[i]]->steps_done + 1 == S->reqs[S->slots[i]]->nsteps) fin.push_back((int)i);
+          if (act[i] && !S->ctx->dead[i] && S->reqs[S->slots[i]]->steps_done + 1 == S->reqs[S->slots[i]]->nsteps)
+            fin.push_back((int)i);
       }
       std::map<int, std::pair<std::vector<double>, std::vector<double>>> states;
       for (int i : fin) {
@@ -312,6 +314,15 @@ void worker_main(cs_server* S) {
         if (r.t_first < 0) {
           r.t_first = t_start;
           S->admit_ms.push_back((float)(1e3 * (t_start - r.t_submit)));
+        }
+        if (S->ctx->dead[i]) {
+          r.status = CS_ERR_DIVERGED;
+          r.done = true;
+          r.t_done = now;
+          S->finished++;
+          S->diverged++;
+          fin.push_back((int)i);
+          continue;
         }
         r.steps_done++;
         r.step_ms.push_back(ms);
@@ -469,6 +480,7 @@ int cs_server_get_stats(cs_server* S, cs_server_stats* st) {
   st->queued = (int)S->queue.size();
   for (int rid : S->slots) st->resident += S->reqs[rid]->done ? 0 : 1;
   st->rebuilds = S->rebuilds;
+  st->diverged = S->diverged;
   st->elapsed_s = seconds_since(S->t0);
   st->busy_s = S->busy_s;
   st->step_ms_p50 = percentile(S->samples, 0.50);

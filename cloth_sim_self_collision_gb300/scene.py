@@ -186,10 +186,11 @@ def config_serving(count: int, seed: int = 11, n_lo: float = 1.0e2, n_hi: float 
     uniform about z, sphere radius uniform in [0.1, 0.4] m, clearance 0.01 m, CG
     tol 1e-6.
 
-    Sheets are 1 m wide up to 81 vertices a side and grow beyond that so their
-    edges stay 1/80 m long: with edges shorter than about 1.4 clearances the
-    reference's proximity test fires between neighbouring cells of a flat sheet,
-    and below 1 cm its edge-edge CCD (whose distance test is fixed at 1e-2) does.
+    Sheets are 1 m wide up to 61 vertices a side and grow beyond that so their
+    edges stay 1/60 m long: when a cell's diagonal spacing (edge / sqrt(2)) is
+    below the clearance the reference's proximity test fires between
+    neighbouring cells of a flat sheet, and below 1 cm its edge-edge CCD (whose
+    distance test is fixed at 1e-2) does.
     Material and time step are the reference demo's (self_contact_sparse/main.cpp:
     lambda 0, mu 30, bending 1e-2, areal density 0.04, dt 0.01, gravity
     (0, 0.05, -10), contact stiffness 300): with the batched sheets' material
@@ -200,7 +201,7 @@ def config_serving(count: int, seed: int = 11, n_lo: float = 1.0e2, n_hi: float 
     for i in range(count):
         n = math.exp(math.log(n_lo) + (math.log(n_hi) - math.log(n_lo)) * r[i, 0])
         side = max(3, int(round(math.sqrt(n))))
-        out.append(square_cloth(side, max(1.0, (side - 1) / 80.0), 0.3 + 1.2 * r[i, 1],
+        out.append(square_cloth(side, max(1.0, (side - 1) / 60.0), 0.3 + 1.2 * r[i, 1],
                                 sphere_radius=0.1 + 0.3 * r[i, 3], clearance=0.01,
                                 rotation=2.0 * math.pi * r[i, 2], seed=5000 + i, density=0.04, lam=0.0,
                                 myu=30.0, stiff_bend=1.0e-2, dt=0.01, gravity=(0.0, 0.05, -10.0),

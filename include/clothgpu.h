@@ -30,6 +30,9 @@ extern "C" {
 #define CS_ERR_OOM 4          /* device allocation failed                            */
 #define CS_ERR_CAPACITY 5     /* a caller-supplied output buffer is too small        */
 #define CS_ERR_TIMEOUT 6      /* a bounded device wait gave up                        */
+#define CS_ERR_DIVERGED 7     /* a cloth blew up (a speed above 1000 m/s after its implicit
+                                 step, or more than 512 overlapping leaf pairs for one
+                                 triangle); it is no longer stepped                    */
 
 /* precision of the implicit solve */
 #define CS_PREC_FP64 0        /* plain: FP64 throughout, bit-exact with the reference */
@@ -88,6 +91,7 @@ typedef struct {
   int impulse_applied;
   int ilu_singular;
   double solver_conv;
+  int diverged;             /* 1 once the cloth blew up (see CS_ERR_DIVERGED)          */
 } cs_stats;
 
 typedef struct cs_ctx cs_ctx;
@@ -239,6 +243,7 @@ typedef struct cs_request_info {
 typedef struct cs_server_stats {
   long long frames, vertex_steps;
   int submitted, finished, queued, resident, rebuilds;
+  int diverged;                              /* requests ended by CS_ERR_DIVERGED        */
   double elapsed_s, busy_s;                  /* since creation; inside frames           */
   double step_ms_p50, step_ms_p99, step_ms_max;  /* over (scene, frame) samples        */
   double admit_ms_p50, admit_ms_p99;         /* submission to first frame               */

@@ -122,3 +122,48 @@ def test_device_bytes_estimate():
     used = f1 - f2
     est = scene_device_bytes(big) - scene_device_bytes(tiny)
     assert 0.65 * used < est < 1.35 * used, (used, est)
+
+
+def _wild(cloth, seed=0):
+    """Initial velocities of 1e4 m/s in random directions: the cloth's swept boxes
+    overlap everywhere at its first CCD pass, the host-made stand-in for a scene
+    whose frames blew up."""
+    return np.random.default_rng(seed).uniform(-1e4, 1e4, 3 * cloth.np)
+
+
+def test_blown_up_cloth_is_isolated_in_a_context():
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    cg = dict(solver_kind=scene.SOLVER_CG, tol=1e-6, maxit=1000)
+    good = scene.square_cloth(21, 1.0, 0.45, sphere_radius=0.3, seed=1, **cg)
+    bad = scene.square_cloth(31, 1.0, 0.6, sphere_radius=0.2, seed=2, **cg)
+    ref = _alone(good, 12, "mixed")
+    ctx = ClothContext(0, "mixed")
+    ig = ctx.add_cloth(good)
+    ib = ctx.add_cloth(bad)
+    ctx.set_state(ib, v=_wild(bad))
+    ctx.step(12)
+    x, v = ctx.get_state(ig)
+    sg, sb = ctx.stats(ig), ctx.stats(ib)
+    ctx.close()
+    assert sb["diverged"] == 1 and sg["diverged"] == 0
+    assert np.array_equal(x, ref[0]) and np.array_equal(v, ref[1])
+
+
+def test_blown_up_scene_fails_alone():
+    """In a server, the blown-up scene ends with CS_ERR_DIVERGED and the scene
+    sharing its arena finishes exactly as it does alone."""
+    from cloth_sim_self_collision_gb300.serve import Server
+    cg = dict(solver_kind=scene.SOLVER_CG, tol=1e-6, maxit=1000)
+    good = scene.square_cloth(21, 1.0, 0.45, sphere_radius=0.3, seed=1, **cg)
+    bad = scene.square_cloth(31, 1.0, 0.6, sphere_radius=0.2, seed=2, **cg)
+    ref = _alone(good, 20, "mixed")
+    with Server(0, "mixed", hbm_budget_bytes=16e9) as srv:
+        rg = srv.submit(good, 20)
+        rb = srv.submit(bad, 20, v=_wild(bad))
+        x, v, info = srv.wait(rg, timeout=600)
+        with pytest.raises(N.CsError) as e:
+            srv.wait(rb, timeout=600)
+        assert e.value.code == N.CS_ERR_DIVERGED
+        st = srv.stats()
+    assert st["diverged"] == 1 and st["finished"] == 2
+    assert np.array_equal(x, ref[0]) and np.array_equal(v, ref[1])
