@@ -200,14 +200,14 @@ def plain_one_per_launch(cloths, device, frames: int, budget_s: float = 8.0) -> 
                       f"inner products), frames 2..{frames + 1}"}
 
 
-def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, plain_frames: int = 10,
-            plain_scenes: int = 6) -> dict:
+def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, plain_budget_s: float = 40.0) -> dict:
     """The serving workload: scenes of log-uniform size (1e2..1e5 vertices) arriving
     as a Poisson process, each run for `steps` frames by the native server (one
     arena, continuous batching, admission by a 150 GB device-byte budget).
     Throughput counts the vertex-steps of scenes that finished; scenes whose frames
-    blew up (CS_ERR_DIVERGED) are counted apart.  The plain FP64 path runs a
-    sample of the same scenes one per context, for `plain_frames` frames each."""
+    blew up (CS_ERR_DIVERGED) are counted apart.  The plain FP64 path runs the
+    same scenes, in arrival order, one per context for the same `steps` frames,
+    until `plain_budget_s` of device time is used."""
     import torch
 
     from cloth_sim_self_collision_gb300 import _native as N
@@ -239,21 +239,24 @@ def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, pl
     # the plain FP64 path, one scene per context, on a sample of the same scenes
     ctx = ClothContext(device, "fp64")
     stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
-    pv, pms, used = 0, 0.0, 0
-    for c in cl[:plain_scenes]:
+    pv, pms, used, tried = 0, 0.0, 0, 0
+    for c in cl:
         cid = ctx.add_cloth(c)
-        ctx.step(1)
         ctx.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        ctx.step(plain_frames)
+        ctx.step(steps)
         e1.record(stream)
         torch.cuda.synchronize()
+        tried += 1
+        ms = e0.elapsed_time(e1)
         if not ctx.stats(cid)["diverged"]:
-            pms += e0.elapsed_time(e1)
-            pv += c.np * plain_frames
+            pms += ms
+            pv += c.np * steps
             used += 1
         ctx.remove_cloth(cid)
+        if pms / 1e3 > plain_budget_s:
+            break
     ctx.close()
     out = {
         "workload": f"{scenes} scenes, vertex count log-uniform 1e2..1e5 (square grids), Poisson arrivals at "
@@ -267,8 +270,8 @@ def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, pl
         "swap_ms_total": st["install_ms_total"], "peak_bytes": st["peak_bytes"],
         "plain_gpu_fp64_one_per_launch": {
             "value": pv / (pms / 1e3) if pms > 0 else None, "unit": UNIT,
-            "sample": f"first {plain_scenes} scenes ({used} that did not blow up), each alone in its own arena, "
-                      f"frames 2..{plain_frames + 1}"},
+            "sample": f"first {tried} scenes in arrival order ({used} that did not blow up), each alone in its "
+                      f"own arena for its {steps} frames"},
     }
     if out["vertex_steps_per_s"] and out["plain_gpu_fp64_one_per_launch"]["value"]:
         out["vs_plain_gpu"] = out["vertex_steps_per_s"] / out["plain_gpu_fp64_one_per_launch"]["value"]

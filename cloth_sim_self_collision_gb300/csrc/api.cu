@@ -374,6 +374,7 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
           pb[k] += 40LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l] + 1) + 168;
       }
       A.slice_pbytes = m.upload(pb, s);
+
       A.p32b = m.alloc<float>(3 * (size_t)NV);
       A.grid_bar = m.alloc<unsigned int>(4);
       CK(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s));

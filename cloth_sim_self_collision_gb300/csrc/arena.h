@@ -50,8 +50,11 @@ struct InstState {
   int total_iters;   // inner iterations summed over refinement cycles
   int cycles;        // refinement cycles
   double red[3];     // per-cloth totals of the slice partials: p.q, r.z, r.r
-  // persistent inner solve: r.z of the iterations by parity
+  // persistent inner solve: r.z of the iterations by parity; istop is set in
+  // phase A when the cloth converges and copied to idone in phase B, so each
+  // phase's skip test reads a flag that no block changes during that phase
   double rzh[2];
+  int istop, ipad;
 };
 
 struct Arena {

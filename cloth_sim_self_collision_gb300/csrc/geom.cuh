@@ -311,6 +311,88 @@ CS_HD bool ee_proximity(int i0, int i1, int j0, int j1, V3<double> p0, V3<double
   return true;
 }
 
+// Conservative FP32 rejection for ee_proximity (edges p = a0 a1, q = b0 b1).
+// Each argument points at a vertex's FP32 bounds (lo[3], hi[3]) around its
+// FP64 position.  Returns true only when the FP64 test certainly rejects the
+// pair: its non-parallel branch is taken (|vp x vq|^2 = det > 1e-20) and the
+// lines' closest points fall outside one of the segments (rp or rq outside
+// [0, 1]), or the lines are farther apart than delta.  Every FP32 quantity
+// carries an error bound (coordinates within one ulp of the FP64 position,
+// then each product and sum rounded separately); decisions need twice that
+// bound as margin, which also covers the rounding of the FP64 evaluation.
+__device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1, const float* b0, const float* b1,
+                                                float delta_hi) {
+  const float u = 5.9604645e-8f;  // 2^-24
+  float X = 0.f;
+#pragma unroll
+  for (int k = 0; k < 6; k++)
+    X = fmaxf(X, fmaxf(fmaxf(fabsf(a0[k]), fabsf(a1[k])), fmaxf(fabsf(b0[k]), fabsf(b1[k]))));
+  float vp[3], vq[3], w[3], D = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    vp[k] = a1[k] - a0[k];
+    vq[k] = b1[k] - b0[k];
+    w[k] = b0[k] - a0[k];
+    D = fmaxf(D, fmaxf(fabsf(vp[k]), fmaxf(fabsf(vq[k]), fabsf(w[k]))));
+  }
+  // component error of the differences: two coordinates within an ulp each
+  // (ulp <= 2^-23 |x|), plus the rounding of the subtraction
+  const float E = 1.001f * (4.0f * u * X + u * D);
+  // t = a . b with its error bound
+  auto dot_err = [&](const float* a, const float* b, float& t, float& e) {
+    float s = 0.f, l1a = 0.f, l1b = 0.f, sab = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float m = a[k] * b[k];
+      s = s + m;
+      l1a += fabsf(a[k]);
+      l1b += fabsf(b[k]);
+      sab += fabsf(m);
+    }
+    t = s;
+    e = 1.001f * (E * (l1a + l1b) + 3.0f * E * E + 3.1f * u * sab);
+  };
+  float t0, t1, t2, t3, t4, e0, e1, e2, e3, e4;
+  dot_err(vp, vp, t0, e0);
+  dot_err(vq, vq, t1, e1);
+  dot_err(vp, vq, t2, e2);
+  dot_err(vp, w, t3, e3);
+  dot_err(vq, w, t4, e4);
+  const float A0 = fabsf(t0) + e0, A1 = fabsf(t1) + e1, A2 = fabsf(t2) + e2, A3 = fabsf(t3) + e3,
+              A4 = fabsf(t4) + e4;
+  const float det = t0 * t1 - t2 * t2;
+  const float edet = 1.001f * (A0 * e1 + A1 * e0 + 2.0f * A2 * e2 + 2.1f * u * (A0 * A1 + A2 * A2) + u * fabsf(det));
+  const float np = t1 * t3 - t2 * t4;
+  const float enp = 1.001f * (A1 * e3 + A3 * e1 + A2 * e4 + A4 * e2 + 2.1f * u * (A1 * A3 + A2 * A4) + u * fabsf(np));
+  const float nq = t2 * t3 - t0 * t4;
+  const float enq = 1.001f * (A2 * e3 + A3 * e2 + A0 * e4 + A4 * e0 + 2.1f * u * (A2 * A3 + A0 * A4) + u * fabsf(nq));
+  // certainly the non-parallel branch of dist_edge_edge
+  if (!(det - 2.0f * edet > 2.0e-20f)) return false;
+  const float dhi = (det + 2.0f * edet) * 1.000001f;
+  if (np + 2.0f * enp < 0.f || np - 2.0f * enp > dhi) return true;  // rp < 0 or rp > 1
+  if (nq + 2.0f * enq < 0.f || nq - 2.0f * enq > dhi) return true;  // rq < 0 or rq > 1
+  // line distance |w . n| / |n| with n = vp x vq, |n|^2 = det; only for well
+  // conditioned pairs (closest points within the segments' span, angle not tiny)
+  if (fabsf(np) > 2.0f * det || fabsf(nq) > 2.0f * det || det < 1.0e-4f * t0 * t1) return false;
+  float n[3], en[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int i = (k + 1) % 3, j = (k + 2) % 3;
+    n[k] = vp[i] * vq[j] - vp[j] * vq[i];
+    en[k] = 1.001f * (E * (fabsf(vp[i]) + fabsf(vq[j]) + fabsf(vp[j]) + fabsf(vq[i])) + 2.0f * E * E +
+                      2.1f * u * (fabsf(vp[i] * vq[j]) + fabsf(vp[j] * vq[i])));
+  }
+  float s = 0.f, es = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    s = s + w[k] * n[k];
+    es += (fabsf(w[k]) + E) * en[k] + E * fabsf(n[k]) + 3.1f * u * fabsf(w[k] * n[k]);
+  }
+  es *= 1.001f;
+  const float sl = fabsf(s) - 2.0f * es;
+  return sl > 0.f && sl * sl > delta_hi * delta_hi * dhi * 1.00001f;
+}
+
 CS_HD bool fv_ccd(int i0, int i1, int i2, int i3, V3<double> p0, V3<double> p1, V3<double> p2, V3<double> p3,
                   V3<double> q0, V3<double> q1, V3<double> q2, V3<double> q3, const Box& bb) {
   const double eps = 1.0e-10;

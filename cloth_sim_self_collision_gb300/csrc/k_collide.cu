@@ -373,6 +373,8 @@ __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, cons
         if (__fadd_ru(qhi, du) < plo) return;  // q + delta < p for all four combinations
         if (__fsub_rd(qlo, du) > phi) return;  // q - delta > p for all four combinations
       }
+      // closest points of the lines outside a segment, or lines too far apart
+      if (ee_prx_reject32(a0, a1, b0, b1, du)) return;
     }
   }
   count_fp64_test(A, ccd ? 5 : 3);

@@ -231,8 +231,10 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
 //   B: from the p.q partials, alpha = r.z / p.q per cloth (again computed by
 //      every block that needs it), then d += alpha p, r -= alpha q,
 //      z = D^-1 r, and the slice partials of r.z and r.r.
-// The block holding a cloth's first slice records its convergence and
-// decrements the count of cloths still iterating; every block reads that count
+// The block holding a cloth's first slice records its convergence (istop in
+// phase A, copied to idone in phase B, so that each phase's skip test reads a
+// flag no block changes during that phase) and decrements the count of cloths
+// still iterating; every block reads that count
 // right after the barrier that follows phase A (nothing changes it before the
 // next phase A), so all blocks leave the loop together.  The direction buffers
 // alternate between iterations.  Totals are the same fixed-order sums in every
@@ -305,7 +307,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
     for (int inst = c0; inst <= c1; inst++) {
       if (!A.active[inst]) continue;
       InstState& St = A.st[inst];
-      if (St.done || St.idone) continue;
+      if (St.done || St.idone) continue;  // idone changes only in phase B
       const bool owner = s0 <= A.slice_lo[inst] && A.slice_lo[inst] < s1;
       float beta = 0.f;
       if (it > 1) {
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
         cloth_totals(A, inst, 1, 2, sh, tot);
         if (tot[1] <= (double)eta * (double)eta * St.rr_in0 || it - 1 >= cap) {
           if (owner && threadIdx.x == 0) {
-            St.idone = 1;
+            St.istop = 1;
             St.inner_iters = it - 1;
             St.red[1] = tot[0];
             St.red[2] = tot[1];
@@ -373,7 +375,11 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
     for (int inst = c0; inst <= c1; inst++) {
       if (!A.active[inst]) continue;
       InstState& St = A.st[inst];
-      if (St.done || St.idone) continue;
+      if (St.done) continue;
+      if (St.istop) {  // istop changes only in phase A
+        if (s0 <= A.slice_lo[inst] && A.slice_lo[inst] < s1 && threadIdx.x == 0) St.idone = 1;
+        continue;
+      }
       double tot[1];
       cloth_totals(A, inst, 0, 1, sh, tot);
       const float alpha = (float)(St.rzh[it & 1] / tot[0]);
@@ -421,6 +427,7 @@ __global__ void k_mx_pstart(Arena A) {
     S.rzh[1] = rz;  // iteration 1 reads parity 1
     S.rr_in0 = rr;
     S.idone = (rr <= 0.0) ? 1 : 0;
+    S.istop = S.idone;
     S.inner_iters = 0;
     if (!S.idone) atomicAdd(&A.grid_bar[3], 1u);
   }

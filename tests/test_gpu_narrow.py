@@ -1,0 +1,76 @@
+"""Proximity contact sets near the decision boundaries of the narrow phase.
+
+The FP32 prefilters in front of the FP64 tests (outward-rounded boxes,
+directed-rounding slab bounds, and the edge-edge closest-point / line-distance
+filter with its error bounds) may only reject pairs that the reference's FP64
+test rejects.  Crumpled sheets put many edge pairs near every threshold (the
+clearance, the segment ends, near-parallel edges); the contact lists must equal
+the oracle's bit for bit."""
+import numpy as np
+import pytest
+
+from cloth_sim_self_collision_gb300 import scene
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from cloth_sim_self_collision_gb300 import build
+    build.build()
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    c = ClothContext()
+    yield c
+    c.close()
+
+
+def crumpled(c, seed, amp_xy, amp_z):
+    """The sheet's rest shape with a smooth fold plus random jitter: layers and
+    neighbours at distances around the clearance."""
+    rng = np.random.default_rng(seed)
+    X = c.X0.reshape(-1, 3).copy()
+    X[:, 2] += 0.05 * np.sin(7.0 * X[:, 0]) * np.cos(5.0 * X[:, 1])
+    X[:, :2] += rng.uniform(-amp_xy, amp_xy, (len(X), 2))
+    X[:, 2] += rng.uniform(-amp_z, amp_z, len(X))
+    return X.reshape(-1)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_prx_contacts_crumpled(ctx, oracle_port, seed):
+    c = scene.square_cloth(31, 0.5, 0.4, sphere_radius=0.2, clearance=0.01, seed=20 + seed,
+                           solver_kind=scene.SOLVER_CG, tol=1e-6, maxit=1000)
+    cid = ctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    x = crumpled(c, seed, amp_xy=0.004 * (1 + seed), amp_z=0.006 * (1 + seed % 3))
+    total = 0
+    for delta in (0.005, 0.01, 0.02, 0.04):
+        a = ctx.contacts_prx(cid, x, delta)
+        b = orc.contacts_prx(x, delta)
+        assert np.array_equal(a, b), (seed, delta, len(a), len(b))
+        total += len(b)
+    ctx.remove_cloth(cid)
+    orc.close()
+    assert total > 0
+
+
+def test_prx_contacts_fold_probe_scaled(ctx, oracle_port):
+    """The folded sheet's probe state squeezed toward its centroid: layers cross
+    the clearance one after another."""
+    import json
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    arr = dict(np.load(os.path.join(here, "golden", "fold_31.npz")))
+    c = scene.square_cloth(31, 1.0, 0.4, sphere_radius=0.2, clearance=0.01, seed=11,
+                           solver_kind=scene.SOLVER_CG, tol=1.0e-6, maxit=1000)
+    cid = ctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    X = arr["probe_x"].reshape(-1, 3)
+    g = X.mean(axis=0)
+    for s in (1.0, 0.9, 0.75, 0.6, 0.5):
+        x = (g + s * (X - g)).reshape(-1)
+        a = ctx.contacts_prx(cid, x, 0.01)
+        b = orc.contacts_prx(x, 0.01)
+        assert np.array_equal(a, b), (s, len(a), len(b))
+    ctx.remove_cloth(cid)
+    orc.close()
