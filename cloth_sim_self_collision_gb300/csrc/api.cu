@@ -36,11 +36,17 @@ void free_contacts(cs_ctx* c) {
   c->C = ContactBufs();
 }
 
-void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t s, int pair_cap, int cand_cap) {
+// q_fv / q_ee: queue capacities of the narrow phase (-1: derived from pair_cap)
+void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t s, int pair_cap, int cand_cap,
+                         int q_fv = -1, int q_ee = -1) {
   C.pair_cap = pair_cap;
   C.cand_cap = cand_cap;
   C.ce_cap = cand_cap;
   C.pairs = m.alloc<int2>(pair_cap);
+  C.q_cap[0] = q_fv > 0 ? q_fv : std::max(pair_cap / 2, 4096);
+  C.q_cap[1] = q_ee > 0 ? q_ee : (int)std::min<long long>(2LL * pair_cap, 0x7fffffffLL);
+  C.queue[0] = m.alloc<int2>(C.q_cap[0]);
+  C.queue[1] = m.alloc<int2>(C.q_cap[1]);
   C.cand = m.alloc<Cand>(cand_cap);
   C.cand_sorted = m.alloc<Cand>(cand_cap);
   C.key_a = m.alloc<unsigned long long>(cand_cap);
@@ -65,9 +71,9 @@ void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t
   CK(cudaMemsetAsync(C.counters, 0, sizeof(int) * 8, s));
 }
 
-void alloc_contacts(cs_ctx* c, int pair_cap, int cand_cap) {
+void alloc_contacts(cs_ctx* c, int pair_cap, int cand_cap, int q_fv = -1, int q_ee = -1) {
   free_contacts(c);
-  alloc_contacts_into(c->A, c->C, c->cmem, c->stream, pair_cap, cand_cap);
+  alloc_contacts_into(c->A, c->C, c->cmem, c->stream, pair_cap, cand_cap, q_fv, q_ee);
   c->token = 0;
 }
 
@@ -635,15 +641,25 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
   for (int attempt = 0;; attempt++) {
     CK(cudaMemsetAsync(c->C.counters + 1, 0, sizeof(int) * 3, s));
     launch_narrow(c->A, c->C, ccd, xs, vs, delta_override, npairs, s);
-    CK(cudaMemcpyAsync(cnt, c->C.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+    int all[8];
+    CK(cudaMemcpyAsync(all, c->C.counters, sizeof(int) * 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    std::memcpy(cnt, all, sizeof(int) * 4);
     if (!cnt[3]) break;
+    // candidates or a test queue overflowed (a queue holds at most 15 tests per pair)
     const long long need = (long long)(unsigned)cnt[1];
-    if (attempt > 4 || need > kMaxCandidates || need < c->C.cand_cap)
+    const long long nfv = (long long)(unsigned)all[6], nee = (long long)(unsigned)all[7];
+    const bool over_c = need >= c->C.cand_cap, over_fv = nfv > c->C.q_cap[0], over_ee = nee > c->C.q_cap[1];
+    if (attempt > 4 || need > kMaxCandidates || nfv > 6LL * npairs || nee > 9LL * npairs ||
+        !(over_c || over_fv || over_ee))
       throw CapacityError("narrow phase: more than " + std::to_string(kMaxCandidates) + " contact candidates");
     const int pairs_keep = c->C.pair_cap;
+    const long long qmax = 0x7fffffffLL;
+    const int q_fv = over_fv ? (int)std::min({2 * nfv + 4096, 6LL * npairs + 4096, qmax}) : c->C.q_cap[0];
+    const int q_ee = over_ee ? (int)std::min({2 * nee + 4096, 9LL * npairs + 4096, qmax}) : c->C.q_cap[1];
     // the pair list must survive the regrow: recompute it after growing
-    alloc_contacts(c, pairs_keep, (int)std::min(2 * need + 4096, kMaxCandidates));
+    alloc_contacts(c, pairs_keep, over_c ? (int)std::min(2 * need + 4096, kMaxCandidates) : c->C.cand_cap, q_fv,
+                   q_ee);
     CK(cudaMemsetAsync(c->C.counters, 0, sizeof(int) * 4, s));
     launch_traverse(c->A, c->C, s);
   }
@@ -867,7 +883,7 @@ size_t cloth_device_bytes(const ClothTopo& t) {
   const size_t sell = ((np + 31) / 32) * 32 * 16;  // SELL entries, padded to the slice width
   b += sell * (36 + 4) + (nb + np) * 8;        // FP32 values, columns, SELL positions
   b += np * (36 + 5 * 12);                     // FP32 diagonal inverse and vectors
-  b += (16 * nt + 4096) * 8 + (4 * nt + 4096) * 120;  // pair and candidate buffers
+  b += (16 * nt + 4096) * 8 * 7 / 2 + (4 * nt + 4096) * 120;  // pair, test-queue and candidate buffers
   b += np * (2 * 4 + 2 * 8 + 72);              // vertex marks, zone keys and sums
   return b + (1 << 16);
 }

@@ -132,6 +132,10 @@ struct Arena {
 struct ContactBufs {
   int pair_cap = 0, cand_cap = 0, ce_cap = 0;
   int2* pairs = nullptr;
+  // elementary tests that passed the FP32 prefilters, waiting for their FP64
+  // test, as (pair index, test index): face-vertex [0] and edge-edge [1]
+  int q_cap[2] = {0, 0};
+  int2* queue[2] = {nullptr, nullptr};
   Cand* cand = nullptr;
   Cand* cand_sorted = nullptr;
   unsigned long long *key_a = nullptr, *key_b = nullptr;
@@ -139,7 +143,8 @@ struct ContactBufs {
   int* ce = nullptr;          // 5 ints per contact, sorted, deduplicated
   int* ce_inst_lo = nullptr;  // per cloth segment of ce
   int* ce_inst_hi = nullptr;
-  int* counters = nullptr;    // [0] pairs, [1] candidates, [2] contacts, [3] overflow flag
+  int* counters = nullptr;    // [0] pairs, [1] candidates, [2] contacts, [3] overflow flag,
+                              // [6] / [7] face-vertex / edge-edge tests queued
   int* level = nullptr;       // impulse level per contact
   int* order = nullptr;       // contacts grouped by level
   int* lev_cnt = nullptr;     // per cloth: level count (then offsets)

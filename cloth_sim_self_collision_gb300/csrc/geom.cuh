@@ -314,12 +314,16 @@ CS_HD bool ee_proximity(int i0, int i1, int j0, int j1, V3<double> p0, V3<double
 // Conservative FP32 rejection for ee_proximity (edges p = a0 a1, q = b0 b1).
 // Each argument points at a vertex's FP32 bounds (lo[3], hi[3]) around its
 // FP64 position.  Returns true only when the FP64 test certainly rejects the
-// pair: its non-parallel branch is taken (|vp x vq|^2 = det > 1e-20) and the
-// lines' closest points fall outside one of the segments (rp or rq outside
-// [0, 1]), or the lines are farther apart than delta.  Every FP32 quantity
-// carries an error bound (coordinates within one ulp of the FP64 position,
-// then each product and sum rounded separately); decisions need twice that
-// bound as margin, which also covers the rounding of the FP64 evaluation.
+// pair.  The FP64 test accepts only with rp, rq in [0, 1] and |pm - qm| <=
+// delta for the points pm, qm at those ratios, which lie on the segments: so
+// any axis along which the two segments are more than delta apart rejects (the
+// edge directions vp and vq, and the common normal vp x vq), in either branch
+// of dist_edge_edge.  When its non-parallel branch is certain
+// (|vp x vq|^2 = det > 1e-20), closest-point ratios certainly outside [0, 1]
+// reject as well.  Every FP32 quantity carries an error bound (coordinates
+// within one ulp of the FP64 position, then each product and sum rounded
+// separately); decisions need twice that bound as margin, which also covers
+// the rounding of the FP64 evaluation.
 __device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1, const float* b0, const float* b1,
                                                 float delta_hi) {
   const float u = 5.9604645e-8f;  // 2^-24
@@ -360,20 +364,35 @@ __device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1
   dot_err(vq, w, t4, e4);
   const float A0 = fabsf(t0) + e0, A1 = fabsf(t1) + e1, A2 = fabsf(t2) + e2, A3 = fabsf(t3) + e3,
               A4 = fabsf(t4) + e4;
+  const float d2 = delta_hi * delta_hi * 1.00001f;
+  // axis vp: p spans [0, t0] (relative to a0), q spans its two ends t3, t3 + t2
+  {
+    const float q1 = t3 + t2, lo = fminf(t3, q1), hi = fmaxf(t3, q1);
+    const float g = fmaxf(lo - t0, -hi), eg = 1.001f * (e0 + e2 + 2.0f * e3 + u * (fabsf(q1) + A0 + A3));
+    const float gl = g - 2.0f * eg;
+    if (gl > 0.f && gl * gl > d2 * (t0 + 2.0f * e0)) return true;
+  }
+  // axis vq: q spans [0, t1] (relative to b0), p spans its two ends -t4, t2 - t4
+  {
+    const float p1 = t2 - t4, lo = fminf(-t4, p1), hi = fmaxf(-t4, p1);
+    const float g = fmaxf(lo - t1, -hi), eg = 1.001f * (e1 + e2 + 2.0f * e4 + u * (fabsf(p1) + A1 + A4));
+    const float gl = g - 2.0f * eg;
+    if (gl > 0.f && gl * gl > d2 * (t1 + 2.0f * e1)) return true;
+  }
   const float det = t0 * t1 - t2 * t2;
   const float edet = 1.001f * (A0 * e1 + A1 * e0 + 2.0f * A2 * e2 + 2.1f * u * (A0 * A1 + A2 * A2) + u * fabsf(det));
   const float np = t1 * t3 - t2 * t4;
   const float enp = 1.001f * (A1 * e3 + A3 * e1 + A2 * e4 + A4 * e2 + 2.1f * u * (A1 * A3 + A2 * A4) + u * fabsf(np));
   const float nq = t2 * t3 - t0 * t4;
   const float enq = 1.001f * (A2 * e3 + A3 * e2 + A0 * e4 + A4 * e0 + 2.1f * u * (A2 * A3 + A0 * A4) + u * fabsf(nq));
-  // certainly the non-parallel branch of dist_edge_edge
-  if (!(det - 2.0f * edet > 2.0e-20f)) return false;
+  if (!(det - 2.0f * edet > 0.f)) return false;
   const float dhi = (det + 2.0f * edet) * 1.000001f;
-  if (np + 2.0f * enp < 0.f || np - 2.0f * enp > dhi) return true;  // rp < 0 or rp > 1
-  if (nq + 2.0f * enq < 0.f || nq - 2.0f * enq > dhi) return true;  // rq < 0 or rq > 1
-  // line distance |w . n| / |n| with n = vp x vq, |n|^2 = det; only for well
-  // conditioned pairs (closest points within the segments' span, angle not tiny)
-  if (fabsf(np) > 2.0f * det || fabsf(nq) > 2.0f * det || det < 1.0e-4f * t0 * t1) return false;
+  // certainly the non-parallel branch of dist_edge_edge: ratios
+  if (det - 2.0f * edet > 2.0e-20f) {
+    if (np + 2.0f * enp < 0.f || np - 2.0f * enp > dhi) return true;  // rp < 0 or rp > 1
+    if (nq + 2.0f * enq < 0.f || nq - 2.0f * enq > dhi) return true;  // rq < 0 or rq > 1
+  }
+  // axis n = vp x vq (|n|^2 = det): both segments project to single points
   float n[3], en[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -390,7 +409,7 @@ __device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1
   }
   es *= 1.001f;
   const float sl = fabsf(s) - 2.0f * es;
-  return sl > 0.f && sl * sl > delta_hi * delta_hi * dhi * 1.00001f;
+  return sl > 0.f && sl * sl > d2 * dhi;
 }
 
 CS_HD bool fv_ccd(int i0, int i1, int i2, int i3, V3<double> p0, V3<double> p1, V3<double> p2, V3<double> p3,

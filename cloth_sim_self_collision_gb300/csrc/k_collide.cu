@@ -302,33 +302,97 @@ __device__ __forceinline__ void count_fp64_test(const Arena& A, int slot) {
   if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&A.bytes_acc[slot], (unsigned long long)__popc(m));
 }
 
-// Narrow phase (bvh_aabb.cpp:473-536 proximity, 836-901 CCD): one thread per
-// (elementary test, leaf pair), test-major, so that a warp runs one kind of
-// test (the FP64 paths of the 15 tests differ widely).  Tests 0-2: face a vs
-// the vertices of b; 3-5: face b vs the vertices of a; 6-14: the 9 edge pairs.
-__global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs, double delta_override,
-                         int npairs) {
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (tid >= 15LL * npairs) return;
-  const int test = (int)(tid / npairs);
-  const int pid = (int)(tid - (long long)test * npairs);
+// Narrow phase (bvh_aabb.cpp:473-536 proximity, 836-901 CCD) in two passes.
+// Pass 1: one thread per leaf pair runs the FP32 prefilters of the pair's 15
+// elementary tests (0-2: face a vs the vertices of b; 3-5: face b vs the
+// vertices of a; 6-14: the 9 edge pairs).  The prefilters reject only what the
+// FP64 tests reject; the survivors are queued (face-vertex and edge-edge tests
+// apart).  Pass 2: the FP64 tests run on
+// the packed queues, one kind per kernel, so their warps stay full.  The
+// candidates' order does not matter (they are sorted afterwards).
+__device__ __forceinline__ void enqueue(const ContactBufs& C, int kind, int pid, int test) {
+  const int slot = warp_append(&C.counters[6 + kind]);
+  if ((unsigned)slot >= (unsigned)C.q_cap[kind]) {
+    C.counters[3] = 1;
+    return;
+  }
+  C.queue[kind][slot] = make_int2(pid, test);
+}
+
+__global__ void k_narrow_filter(Arena A, ContactBufs C, int ccd, double delta_override, int npairs) {
+  const int pid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pid >= npairs) return;
   const int2 pr = C.pairs[pid];
   const int na = pr.x, nb = pr.y;
   const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
   const int inst = A.tinst[ta];
   if (A.st[inst].diverged) return;
-  const DevParams& P = A.prm[inst];
-  const double delta = delta_override >= 0 ? delta_override : P.contact_clearance;
-  if (test < 6) {
+  const double delta = delta_override >= 0 ? delta_override : A.prm[inst].contact_clearance;
+  const float du = __double2float_ru(delta);
+  const int va[3] = {A.tri[3 * ta], A.tri[3 * ta + 1], A.tri[3 * ta + 2]};
+  const int vb[3] = {A.tri[3 * tb], A.tri[3 * tb + 1], A.tri[3 * tb + 2]};
+  // face-vertex: the vertex inside the face's box (the reference's aBB quirk for
+  // proximity: the node whose index is the triangle's index within its cloth)
+#pragma unroll 1
+  for (int test = 0; test < 6; test++) {
+    const bool fa = test < 3;
+    const int* f = fa ? va : vb;
+    const int q = fa ? vb[test] : va[test - 3];
+    if (q == f[0] || q == f[1] || q == f[2]) continue;
+    const int tf = fa ? ta : tb;
+    const int bn = ccd ? (fa ? na : nb) : A.noff[inst] + (tf - A.toff[inst]);
+    if (!overlap32(A.box32 + 6 * (size_t)bn, A.vb32 + 6 * (size_t)q)) continue;
+    enqueue(C, 0, pid, test);
+  }
+#pragma unroll 1
+  for (int k = 0; k < 9; k++) {
+    const int i0 = va[kEE[k][0]], i1 = va[kEE[k][1]];
+    const int j0 = vb[kEE[k][2]], j1 = vb[kEE[k][3]];
+    if (i0 == j0 || i0 == j1 || i1 == j0 || i1 == j1) continue;
+    // for CCD the edges' swept boxes must overlap; for proximity the reference's
+    // six slab tests (bvh_aabb.cpp:420-425) are bounded with directed rounding,
+    // then the closest-point / distance filter
+    const float *a0 = A.vb32 + 6 * (size_t)i0, *a1 = A.vb32 + 6 * (size_t)i1;
+    const float *b0 = A.vb32 + 6 * (size_t)j0, *b1 = A.vb32 + 6 * (size_t)j1;
+    bool keep = true;
+    if (ccd) {
+      float ea[6], eb[6];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        ea[c] = fminf(a0[c], a1[c]);
+        ea[3 + c] = fmaxf(a0[3 + c], a1[3 + c]);
+        eb[c] = fminf(b0[c], b1[c]);
+        eb[3 + c] = fmaxf(b0[3 + c], b1[3 + c]);
+      }
+      keep = overlap32(ea, eb);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const float plo = fminf(a0[c], a1[c]), phi = fmaxf(a0[3 + c], a1[3 + c]);
+        const float qlo = fminf(b0[c], b1[c]), qhi = fmaxf(b0[3 + c], b1[3 + c]);
+        if (__fadd_ru(qhi, du) < plo || __fsub_rd(qlo, du) > phi) keep = false;
+      }
+      if (keep && ee_prx_reject32(a0, a1, b0, b1, du)) keep = false;
+    }
+    if (keep) enqueue(C, 1, pid, 6 + k);
+  }
+}
+
+// pass 2, face-vertex tests (grid-stride over their queue)
+__global__ void k_narrow_fv(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs,
+                            double delta_override) {
+  const int n = min(__ldcg(&C.counters[6]), C.q_cap[0]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 it = C.queue[0][i];
+    const int2 pr = C.pairs[it.x];
+    const int na = pr.x, nb = pr.y, test = it.y;
+    const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
+    const int inst = A.tinst[ta];
+    const DevParams& P = A.prm[inst];
+    const double delta = delta_override >= 0 ? delta_override : P.contact_clearance;
     const bool fa = test < 3;
     const int tf = fa ? ta : tb, tv = fa ? tb : ta, k = fa ? test : test - 3;
     const int f0 = A.tri[3 * tf], f1 = A.tri[3 * tf + 1], f2 = A.tri[3 * tf + 2], q = A.tri[3 * tv + k];
-    if (q == f0 || q == f1 || q == f2) return;
-    // FP32 prefilter: rejects only what the FP64 box test rejects (outward boxes)
-    {
-      const int bn = ccd ? (fa ? na : nb) : A.noff[inst] + (tf - A.toff[inst]);
-      if (!overlap32(A.box32 + 6 * (size_t)bn, A.vb32 + 6 * (size_t)q)) return;
-    }
     count_fp64_test(A, ccd ? 4 : 2);
     const V3<double> p0 = ld3(xs, f0), p1 = ld3(xs, f1), p2 = ld3(xs, f2), p3 = ld3(xs, q);
     if (!ccd) {
@@ -342,49 +406,33 @@ __global__ void k_narrow(Arena A, ContactBufs C, int ccd, const double* xs, cons
                  end_pos(xs, vs, f2, P.dt), end_pos(xs, vs, q, P.dt), bb))
         emit(C, 1, f0, f1, f2, q, na, nb, test);
     }
-    return;
   }
-  const int k = test - 6;
-  const int i0 = A.tri[3 * ta + kEE[k][0]], i1 = A.tri[3 * ta + kEE[k][1]];
-  const int j0 = A.tri[3 * tb + kEE[k][2]], j1 = A.tri[3 * tb + kEE[k][3]];
-  if (i0 == j0 || i0 == j1 || i1 == j0 || i1 == j1) return;
-  {
-    // FP32 prefilter on outward bounds: for CCD the edges' swept boxes must
-    // overlap; for proximity the reference's six slab tests (bvh_aabb.cpp:420-425)
-    // are bounded with directed rounding, so a rejection here is a rejection in FP64
-    const float *a0 = A.vb32 + 6 * (size_t)i0, *a1 = A.vb32 + 6 * (size_t)i1;
-    const float *b0 = A.vb32 + 6 * (size_t)j0, *b1 = A.vb32 + 6 * (size_t)j1;
-    if (ccd) {
-      float ea[6], eb[6];
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        ea[k] = fminf(a0[k], a1[k]);
-        ea[3 + k] = fmaxf(a0[3 + k], a1[3 + k]);
-        eb[k] = fminf(b0[k], b1[k]);
-        eb[3 + k] = fmaxf(b0[3 + k], b1[3 + k]);
-      }
-      if (!overlap32(ea, eb)) return;
+}
+
+// pass 2, edge-edge tests (grid-stride over their queue)
+__global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs,
+                            double delta_override) {
+  const int n = min(__ldcg(&C.counters[7]), C.q_cap[1]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 it = C.queue[1][i];
+    const int2 pr = C.pairs[it.x];
+    const int na = pr.x, nb = pr.y, test = it.y;
+    const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
+    const int inst = A.tinst[ta];
+    const DevParams& P = A.prm[inst];
+    const double delta = delta_override >= 0 ? delta_override : P.contact_clearance;
+    const int k = test - 6;
+    const int i0 = A.tri[3 * ta + kEE[k][0]], i1 = A.tri[3 * ta + kEE[k][1]];
+    const int j0 = A.tri[3 * tb + kEE[k][2]], j1 = A.tri[3 * tb + kEE[k][3]];
+    count_fp64_test(A, ccd ? 5 : 3);
+    const V3<double> p0 = ld3(xs, i0), p1 = ld3(xs, i1), q0 = ld3(xs, j0), q1 = ld3(xs, j1);
+    if (!ccd) {
+      if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
     } else {
-      const float du = __double2float_ru(delta);
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        const float plo = fminf(a0[k], a1[k]), phi = fmaxf(a0[3 + k], a1[3 + k]);
-        const float qlo = fminf(b0[k], b1[k]), qhi = fmaxf(b0[3 + k], b1[3 + k]);
-        if (__fadd_ru(qhi, du) < plo) return;  // q + delta < p for all four combinations
-        if (__fsub_rd(qlo, du) > phi) return;  // q - delta > p for all four combinations
-      }
-      // closest points of the lines outside a segment, or lines too far apart
-      if (ee_prx_reject32(a0, a1, b0, b1, du)) return;
+      if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, end_pos(xs, vs, i0, P.dt), end_pos(xs, vs, i1, P.dt),
+                 end_pos(xs, vs, j0, P.dt), end_pos(xs, vs, j1, P.dt)))
+        emit(C, 0, i0, i1, j0, j1, na, nb, test);
     }
-  }
-  count_fp64_test(A, ccd ? 5 : 3);
-  const V3<double> p0 = ld3(xs, i0), p1 = ld3(xs, i1), q0 = ld3(xs, j0), q1 = ld3(xs, j1);
-  if (!ccd) {
-    if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
-  } else {
-    if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, end_pos(xs, vs, i0, P.dt), end_pos(xs, vs, i1, P.dt),
-               end_pos(xs, vs, j0, P.dt), end_pos(xs, vs, j1, P.dt)))
-      emit(C, 0, i0, i1, j0, j1, na, nb, test);
   }
 }
 
@@ -873,10 +921,20 @@ void launch_mark_dirty(const Arena& A, const ContactBufs& C, int nce, bool zones
 void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
                    double delta_override, int npairs, cudaStream_t s) {
   if (npairs <= 0) return;
+  static int grid2 = 0;
+  if (grid2 == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid2 = 8 * (sms > 0 ? sms : 1);
+  }
   prof_begin(PK_NARROW, s);
-  k_narrow<<<nblk(15LL * npairs), kT, 0, s>>>(A, C, ccd, xs, vs, delta_override, npairs);
+  cudaMemsetAsync(C.counters + 6, 0, 2 * sizeof(int), s);
+  k_narrow_filter<<<nblk(npairs), kT, 0, s>>>(A, C, ccd, delta_override, npairs);
+  k_narrow_fv<<<grid2, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
+  k_narrow_ee<<<grid2, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
   prof_end(PK_NARROW, s);
-  g_launches++;
+  g_launches += 3;
 }
 
 size_t cub_sort_bytes(int n) {
