@@ -40,6 +40,7 @@ EXPORTS = [
     "cs_profile", "cs_profile_read", "cs_stream", "cs_profile_bytes", "cs_get_boxes", "cs_solve_cg_noalloc",
     "cs_server_create", "cs_server_submit", "cs_server_wait", "cs_server_release", "cs_server_drain",
     "cs_server_get_stats", "cs_server_last_error", "cs_server_destroy", "cs_scene_device_bytes",
+    "cs_vertex_normals",
 ]
 
 
@@ -200,6 +201,7 @@ def load(path: str | None = None, build_if_missing: bool = False):
     f("cs_server_last_error", ctypes.c_char_p, _V)
     f("cs_server_destroy", None, _V)
     f("cs_scene_device_bytes", ctypes.c_size_t, i, _D, i, _I, i, _I, P)
+    f("cs_vertex_normals", i, _V, i, _D, _D)
     _lib = L
     return L
 

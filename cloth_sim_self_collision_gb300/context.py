@@ -146,6 +146,18 @@ class ClothContext:
         self._ck(self.L.cs_update_velocity(self.h, cid, N.dp(x), N.dp(v)))
         return v
 
+    def vertex_normals(self, cid: int = -1, x=None):
+        """MakeNormal (self_contact_sparse/main.cpp:183-211): unit vertex normals of
+        cloth cid at positions x (default: its state), or of every cloth (cid = -1)."""
+        if cid < 0:
+            out = np.empty(3 * self.num_vertices())
+            self._ck(self.L.cs_vertex_normals(self.h, -1, None, N.dp(out)))
+            return out
+        out = np.empty(3 * self.np[cid])
+        xa = None if x is None else np.ascontiguousarray(x, np.float64)
+        self._ck(self.L.cs_vertex_normals(self.h, cid, None if xa is None else N.dp(xa), N.dp(out)))
+        return out
+
     def pattern(self, cid):
         nb = ctypes.c_int()
         self._ck(self.L.cs_pattern(self.h, cid, ctypes.byref(nb), None, None))

@@ -1532,6 +1532,30 @@ int cs_get_states(cs_ctx* c, double* x, double* v) {
   });
 }
 
+int cs_vertex_normals(cs_ctx* c, int id, const double* x, double* normals) {
+  return guarded(c, [&] {
+    if (!normals) throw ArgError("null normals");
+    if (id < 0 && x) throw ArgError("positions are per cloth: pass id >= 0 with x");
+    ensure(c);
+    const Arena& A = c->A;
+    if (A.ni == 0) return;
+    // dx is a work vector of the implicit step: free between frames
+    if (id >= 0) {
+      const int i = slot_of(c, id);
+      const size_t n = 3 * (size_t)c->cloths[id]->topo.np, off = 3 * (size_t)c->voff[i];
+      if (x) up(c, A.x1 + off, x, n);
+      set_active(c, only(c, i));
+      launch_vertex_normals(A, x ? A.x1 : A.x, A.dx, c->stream);
+      down(c, normals, A.dx + off, n);
+    } else {
+      set_active(c, std::vector<int>(A.ni, 1));
+      launch_vertex_normals(A, A.x, A.dx, c->stream);
+      down(c, normals, A.dx, 3 * (size_t)A.nv);
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
 long long cs_num_vertices(const cs_ctx* c) {
   if (!c) return 0;
   long long n = 0;

@@ -235,6 +235,40 @@ __global__ void k_update_velocity(Arena A) {
   }
 }
 
+// MakeNormal (self_contact_sparse/main.cpp:183-211): per vertex, the unit
+// normals (UnitNormalAreaTri3D, utility.h:58-73) of its triangles added in
+// triangle order (the vertex's gradient sources list them ascending), then the
+// sum scaled by 1 / sqrt(|sum|^2): the reference's operations, in its order.
+__global__ void k_vertex_normals(Arena A, const double* xs, double* out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv || !A.active[A.vinst[v]]) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int e = A.grad_ptr[v]; e < A.grad_ptr[v + 1]; e++) {
+    const int code = A.grad_src[e];
+    if (code < 0) continue;  // a bending stencil
+    const int t = code / 3;
+    const double* a = xs + 3 * A.tri[3 * t];
+    const double* b = xs + 3 * A.tri[3 * t + 1];
+    const double* c = xs + 3 * A.tri[3 * t + 2];
+    double n0 = (b[1] - a[1]) * (c[2] - a[2]) - (c[1] - a[1]) * (b[2] - a[2]);
+    double n1 = (b[2] - a[2]) * (c[0] - a[0]) - (c[2] - a[2]) * (b[0] - a[0]);
+    double n2 = (b[0] - a[0]) * (c[1] - a[1]) - (c[0] - a[0]) * (b[1] - a[1]);
+    const double area = sqrt(n0 * n0 + n1 * n1 + n2 * n2) * 0.5;
+    const double inv = 0.5 / area;
+    n0 *= inv;
+    n1 *= inv;
+    n2 *= inv;
+    s0 += n0;
+    s1 += n1;
+    s2 += n2;
+  }
+  const double sq = s0 * s0 + s1 * s1 + s2 * s2;
+  const double inv = 1.0 / sqrt(sq);
+  out[3 * v + 0] = s0 * inv;
+  out[3 * v + 1] = s1 * inv;
+  out[3 * v + 2] = s2 * inv;
+}
+
 // x += dx, v = dx / dt; a speed above kMaxSpeed (or not a number) marks the
 // cloth as blown up
 __global__ void k_finish_implicit(Arena A) {
@@ -359,6 +393,11 @@ void launch_update_velocity(const Arena& A, cudaStream_t s) {
 
 void launch_finish_implicit(const Arena& A, cudaStream_t s) {
   k_finish_implicit<<<blocks_for(3LL * A.nv), kThreads, 0, s>>>(A);
+  g_launches++;
+}
+
+void launch_vertex_normals(const Arena& A, const double* xs, double* out, cudaStream_t s) {
+  k_vertex_normals<<<blocks_for(A.nv), kThreads, 0, s>>>(A, xs, out);
   g_launches++;
 }
 

@@ -38,6 +38,8 @@ void launch_slot_reduce(const Arena& A, cudaStream_t s);
 void launch_rhs(const Arena& A, cudaStream_t s);
 void launch_update_velocity(const Arena& A, cudaStream_t s);  // masked
 void launch_finish_implicit(const Arena& A, cudaStream_t s);  // x += dx, v = dx/dt
+// MakeNormal for the active cloths at positions xs into out (3 per vertex)
+void launch_vertex_normals(const Arena& A, const double* xs, double* out, cudaStream_t s);
 void launch_reintegrate(const Arena& A, cudaStream_t s);      // masked: x = x1 + v dt
 void launch_element_batch_cst(int n, const double* C, const double* c, double lambda, double myu, double* W,
                               double* dW, double* ddW, cudaStream_t s);

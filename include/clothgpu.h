@@ -212,6 +212,12 @@ int cs_element_contact(cs_ctx *ctx, int n, const double *c, const cs_params *prm
  * pointer may be null. */
 int cs_set_states(cs_ctx *ctx, const double *x, const double *v);
 int cs_get_states(cs_ctx *ctx, double *x, double *v);
+/* MakeNormal (self_contact_sparse/main.cpp:183-211, the demo's render normals)
+ * into a device-side buffer copied to `normals` (3 doubles per vertex): for
+ * cloth `id` at positions x (null: its current state), or, with id = -1 and
+ * x = null, for every cloth of the context in the order of cs_get_states, in
+ * one launch.  Bit-exact with the reference's loop. */
+int cs_vertex_normals(cs_ctx *ctx, int id, const double *x, double *normals);
 /* Total vertices of the context (length of the state arrays / 3). */
 long long cs_num_vertices(const cs_ctx *ctx);
 

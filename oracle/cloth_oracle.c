@@ -1990,6 +1990,33 @@ done:
   if (st) *st = s;
 }
 
+/* MakeNormal, self_contact_sparse/main.cpp:183-211: every triangle's unit
+ * normal (UnitNormalAreaTri3D) added to its three vertices in triangle order,
+ * then each sum scaled by 1 / sqrt(|sum|^2) */
+void co_vertex_normals(const co_cloth *h, const double *x, double *nrm) {
+  int t, i;
+  for (i = 0; i < 3 * h->np; i++) nrm[i] = 0.0;
+  for (t = 0; t < h->nt; t++) {
+    const int *f = h->tri + 3 * t;
+    double n[3], area;
+    int k;
+    unit_normal_area3(n, &area, x + 3 * f[0], x + 3 * f[1], x + 3 * f[2]);
+    for (k = 0; k < 3; k++) {
+      nrm[3 * f[k] + 0] += n[0];
+      nrm[3 * f[k] + 1] += n[1];
+      nrm[3 * f[k] + 2] += n[2];
+    }
+  }
+  for (i = 0; i < h->np; i++) {
+    double *m = nrm + 3 * i;
+    const double sq = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+    const double inv = 1.0 / sqrt(sq);
+    m[0] *= inv;
+    m[1] *= inv;
+    m[2] *= inv;
+  }
+}
+
 /* UpdateIntermidiateVelocity, solve_internal_sparse.h:329-369 */
 void co_update_velocity(co_cloth *h, const double *x, double *v) {
   const co_params *q = &h->prm;

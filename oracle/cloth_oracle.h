@@ -118,6 +118,8 @@ int co_riz_zones(const co_cloth *h, int *zone_of_vertex);
 void co_riz_apply(co_cloth *h, const double *x, double *v, const double *v0);
 void co_resolve(co_cloth *h, const double *x1, double *v, co_stats *st);
 void co_update_velocity(co_cloth *h, const double *x, double *v);
+/* MakeNormal (self_contact_sparse/main.cpp:183-211): unit vertex normals */
+void co_vertex_normals(const co_cloth *h, const double *x, double *nrm);
 
 /* one frame of self_contact_sparse/main.cpp StepTime, in place on x, v */
 void co_step(co_cloth *h, double *x, double *v, co_stats *st);

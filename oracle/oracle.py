@@ -139,6 +139,7 @@ class OracleLib:
         self.riz_apply = f("riz_apply", None, _V, _D, _D, _D)
         self.resolve = f("resolve", None, _V, _D, _D, S)
         self.update_velocity = f("update_velocity", None, _V, _D, _D)
+        self.vertex_normals = f("vertex_normals", None, _V, _D, _D)
         self.step = f("step", None, _V, _D, _D, S)
 
 
@@ -298,6 +299,12 @@ class OracleCloth:
         v = np.array(v, dtype=np.float64)
         self.L.update_velocity(self.h, _dp(np.ascontiguousarray(x)), _dp(v))
         return v
+
+    def vertex_normals(self, x):
+        """MakeNormal (self_contact_sparse/main.cpp:183-211) at positions x."""
+        out = np.zeros(3 * self.cloth.np)
+        self.L.vertex_normals(self.h, _dp(np.ascontiguousarray(x, dtype=np.float64)), _dp(out))
+        return out
 
     def step(self, nsteps: int = 1):
         stats = []

@@ -474,6 +474,27 @@ void ref_update_velocity(void* p, const double* x, double* v) {
   memcpy(v, aUVW.data(), sizeof(double) * n);
 }
 
+// MakeNormal of self_contact_sparse/main.cpp:183-211 (the GLUT file cannot be
+// compiled here): the reference's UnitNormalAreaTri3D in the demo's loop.
+void ref_vertex_normals(void* p, const double* x, double* nrm) {
+  RefCloth* h = (RefCloth*)p;
+  const int np = (int)h->aXYZ0.size() / 3, ntri = (int)h->aTri.size() / 3;
+  std::vector<double> aNormal(3 * (size_t)np, 0.0);
+  for (int itri = 0; itri < ntri; itri++) {
+    const int ip[3] = {h->aTri[3 * itri], h->aTri[3 * itri + 1], h->aTri[3 * itri + 2]};
+    double n[3], area;
+    UnitNormalAreaTri3D(n, area, x + 3 * ip[0], x + 3 * ip[1], x + 3 * ip[2]);
+    for (int k = 0; k < 3; k++)
+      for (int d = 0; d < 3; d++) aNormal[3 * ip[k] + d] += n[d];
+  }
+  for (int i = 0; i < np; i++) {
+    const double sqlen = +aNormal[3 * i] * aNormal[3 * i] + aNormal[3 * i + 1] * aNormal[3 * i + 1] +
+                         aNormal[3 * i + 2] * aNormal[3 * i + 2];
+    const double invlen = 1.0 / sqrt(sqlen);
+    for (int d = 0; d < 3; d++) nrm[3 * i + d] = aNormal[3 * i + d] * invlen;
+  }
+}
+
 // StepTime of self_contact_sparse/main.cpp:213-263 without the normals (render only).
 void ref_step(void* p, double* x, double* v, co_stats* st) {
   RefCloth* h = (RefCloth*)p;

@@ -289,3 +289,26 @@ def test_batch_matches_single(ctx, oracle_port):
         orc = O.OracleCloth(oracle_port, c)
         orc.step(3)
         assert close(xs, orc.x)
+
+
+def test_vertex_normals_bit_exact(oracle_port):
+    """MakeNormal on the device equals the restatement bit for bit, per cloth and
+    for the whole arena in one launch."""
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    ctx = ClothContext()
+    c1 = fold_scene()
+    c2 = scene.config_small()
+    i1, i2 = ctx.add_cloth(c1), ctx.add_cloth(c2)
+    o1, o2 = O.OracleCloth(oracle_port, c1), O.OracleCloth(oracle_port, c2)
+    o1.step(30)
+    o2.step(30)
+    assert np.array_equal(ctx.vertex_normals(i1, o1.x), o1.vertex_normals(o1.x))
+    ctx.set_state(i1, o1.x, o1.v)
+    ctx.set_state(i2, o2.x, o2.v)
+    allv = ctx.vertex_normals()
+    ids = [i1, i2]
+    order = sorted(ids)  # cloths back to back in the order they were added
+    parts = {i1: o1.vertex_normals(o1.x), i2: o2.vertex_normals(o2.x)}
+    expect = np.concatenate([parts[i] for i in order])
+    assert allv.shape == expect.shape and np.array_equal(allv, expect)
+    ctx.close()

@@ -41,3 +41,18 @@ def test_batch_instances_topology(oracle_port, oracle_ref):
         assert np.array_equal(a.bvh_nodes(), b.bvh_nodes())
         assert a.step(1) == b.step(1)
         assert np.array_equal(a.x, b.x)
+
+
+def test_vertex_normals_match_reference(oracle_port, oracle_ref):
+    """MakeNormal: the restatement equals the reference's UnitNormalAreaTri3D loop
+    bit for bit, on a flat sheet and on a folded state."""
+    from cloth_sim_self_collision_gb300 import scene
+    c = scene.square_cloth(31, 1.0, 0.4, sphere_radius=0.2, clearance=0.01, seed=11,
+                           solver_kind=scene.SOLVER_CG, tol=1.0e-6, maxit=1000)
+    a = O.OracleCloth(oracle_port, c)
+    b = O.OracleCloth(oracle_ref, c)
+    a.step(40)
+    for x in (c.X0, a.x):
+        na, nb = a.vertex_normals(x), b.vertex_normals(x)
+        assert np.array_equal(na, nb)
+        assert np.allclose(np.linalg.norm(na.reshape(-1, 3), axis=1), 1.0)
