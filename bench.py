@@ -146,6 +146,10 @@ def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
     ctx.step(warmup)
     ctx.synchronize()
     torch.cuda.synchronize()
+    # the state at the start of the timed frames (the end-to-end run replays them)
+    x0 = np.empty(3 * nv)
+    v0 = np.empty(3 * nv)
+    ctx.get_states(x0, v0)
     launches0 = ctx.launch_count()
     ctx.profile(True)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
@@ -163,7 +167,7 @@ def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
               "fp64_ee_ccd", "persist_bytes"):
         counts[k] = ctx.profile_read(k)[1]
     ctx.profile(False)
-    return step_ms, prof, counts, ctx.launch_count() - launches0
+    return step_ms, prof, counts, ctx.launch_count() - launches0, (x0, v0)
 
 
 PROFILED = ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit", "traverse",
@@ -278,6 +282,39 @@ def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, pl
     return out
 
 
+def single_cloths(device: int, frames: int = 5, warmup: int = 2) -> dict:
+    """The single-cloth configurations (101x101 sheet of 2 m, 256x256 sheet of
+    2 m): mixed precision against the plain FP64 path on the same cloth, frames
+    warmup+1 .. warmup+frames, CUDA events on the library's stream."""
+    import torch
+
+    from cloth_sim_self_collision_gb300 import scene
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    out = {}
+    for name, make in (("single_101", scene.config_single_101), ("single_256", scene.config_single_256)):
+        row = {}
+        for prec in ("mixed", "fp64"):
+            c = make()
+            ctx = ClothContext(device, prec)
+            cid = ctx.add_cloth(c)
+            ctx.step(warmup)
+            ctx.synchronize()
+            stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.step(frames)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            row[prec] = {"value": c.np * frames / (ms / 1e3), "ms_per_step": ms / frames,
+                         "solver_iterations_last": ctx.stats(cid)["solver_iterations"]}
+            ctx.close()
+        row["vertices"] = c.np
+        row["mixed_vs_fp64"] = row["mixed"]["value"] / row["fp64"]["value"]
+        out[name] = row
+    return out
+
+
 def native(args):
     import torch
 
@@ -310,7 +347,8 @@ def native(args):
         clocks = ClockSampler(local)
         barrier()
         clocks.start()
-        step_ms, prof, counts, launches = timed_batch(ctx, ids, args.steps, args.warmup, stream, nv, PROFILED)
+        step_ms, prof, counts, launches, start = timed_batch(ctx, ids, args.steps, args.warmup, stream, nv,
+                                                             PROFILED)
         clk = clocks.stop()
         barrier()
         total_ms = sum(step_ms)
@@ -323,10 +361,12 @@ def native(args):
                "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
                "prof": prof, "counts": counts, "launches": launches, "clocks": clk, "nv": nv, "nb": nb_total}
         if prec == results.get("headline", prec) or not results:
-            # end to end through the C ABI: pinned host state in, frame, state out
+            # end to end through the C ABI, on the same frames: pinned host state
+            # in, frame, state out
             xs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
             vs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
-            ctx.get_states(xs.numpy(), vs.numpy())
+            xs.numpy()[:] = start[0]
+            vs.numpy()[:] = start[1]
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             e0.record(stream)
@@ -394,6 +434,8 @@ def native(args):
     if plain is not None:
         line["plain_gpu_fp64_one_per_launch"] = plain
         line["vs_plain_gpu"] = head["value"] / plain["value"]
+    if not args.no_single:
+        line["single_cloth"] = single_cloths(local)
     if not args.no_serve:
         line["serving"] = serving(local, args.serve_scenes, args.serve_rate, args.serve_steps)
     if not args.no_cpu:
@@ -488,6 +530,7 @@ def main():
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
                     help="both: mixed is the headline, FP64 batched reported beside it")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving workload")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-cloth configurations")
     ap.add_argument("--serve-scenes", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, scenes per second")
     ap.add_argument("--serve-steps", type=int, default=200)

@@ -509,8 +509,8 @@ void run_cg(cs_ctx* c, const std::vector<int>& cg, double tol, int maxit) {
 // (inner relative residual eta, at most `cap` iterations per cycle).
 void run_mixed(cs_ctx* c, const std::vector<int>& act) {
   const Arena& A = c->A;
-  const float eta = 1.0e-3f;
-  const int cap = 300, maxcycles = 12;
+  const float eta = c->mx_eta;
+  const int cap = c->mx_cap, maxcycles = 12;
   set_active(c, act);
   launch_mx_outer_init(A, c->stream);
   launch_mx_warm_start(A, c->stream);
@@ -923,6 +923,8 @@ int cs_create(int device, int precision, cs_ctx** out) {
   c->launches0 = g_launches;
   if (const char* e = std::getenv("CLOTHGPU_MX_PERSISTENT")) c->mx_persistent = std::atoi(e) != 0;
   if (const char* e = std::getenv("CLOTHGPU_MX_BLOCKS_PER_SM")) c->mx_blocks_per_sm = std::atoi(e);
+  if (const char* e = std::getenv("CLOTHGPU_MX_ETA")) c->mx_eta = (float)std::atof(e);
+  if (const char* e = std::getenv("CLOTHGPU_MX_CAP")) c->mx_cap = std::atoi(e);
   *out = c;
   return CS_OK;
 }
