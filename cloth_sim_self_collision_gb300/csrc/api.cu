@@ -517,7 +517,7 @@ void run_mixed(cs_ctx* c, const std::vector<int>& act) {
   for (int cyc = 0; cyc < maxcycles; cyc++) {
     unsigned gave_up = 0;
     if (c->mx_persistent) {
-      launch_mx_inner_persistent(A, eta, cap, c->mx_blocks_per_sm, c->stream);
+      launch_mx_inner_persistent(A, eta, cap, c->mx_blocks_per_sm, c->mx_threads, c->stream);
       CK(cudaMemcpyAsync(&gave_up, A.grid_bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     } else {
       launch_mx_inner_init(A, c->stream);
@@ -924,6 +924,7 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_MX_PERSISTENT")) c->mx_persistent = std::atoi(e) != 0;
   if (const char* e = std::getenv("CLOTHGPU_MX_BLOCKS_PER_SM")) c->mx_blocks_per_sm = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_ETA")) c->mx_eta = (float)std::atof(e);
+  if (const char* e = std::getenv("CLOTHGPU_MX_THREADS")) c->mx_threads = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_CAP")) c->mx_cap = std::atoi(e);
   *out = c;
   return CS_OK;

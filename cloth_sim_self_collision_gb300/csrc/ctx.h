@@ -107,6 +107,7 @@ struct cs_ctx {
   // launch per kernel and iteration), and its blocks per SM (0: occupancy limit)
   bool mx_persistent = true;
   int mx_blocks_per_sm = 0;
+  int mx_threads = 256;  // threads per block of the persistent solve
   // inner FP32 solve of a refinement cycle: relative residual target and cap
   float mx_eta = 1.0e-3f;
   int mx_cap = 300;

@@ -239,8 +239,6 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
 // next phase A), so all blocks leave the loop together.  The direction buffers
 // alternate between iterations.  Totals are the same fixed-order sums in every
 // block: results depend neither on the launch shape nor on the other cloths.
-constexpr int kPersistThreads = 256;
-constexpr int kPersistWarps = kPersistThreads / 32;
 constexpr unsigned kSpinLimit = 1u << 22;  // ~1 s of polling at the least
 
 // Grid-wide barrier on A.grid_bar with a bounded wait.  Returns false when the
@@ -276,7 +274,9 @@ __device__ bool grid_sync(const Arena& A) {
 
 // Totals over the slices of cloth inst of nf partial fields starting at f0, as
 // fixed-order block sums (every thread gets them in tot[]).
+template <int kPersistThreads>
 __device__ void cloth_totals(const Arena& A, int inst, int f0, int nf, double* sh, double* tot) {
+  constexpr int kPersistWarps = kPersistThreads / 32;
   const int lo = A.slice_lo[inst], hi = A.slice_hi[inst];
   for (int f = 0; f < nf; f++) {
     double v = 0.0;
@@ -292,7 +292,9 @@ __device__ void cloth_totals(const Arena& A, int inst, int f0, int nf, double* s
   }
 }
 
+template <int kPersistThreads>
 __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float eta, int cap) {
+  constexpr int kPersistWarps = kPersistThreads / 32;
   __shared__ double sh[kPersistWarps];
   __shared__ int s_left;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -312,7 +314,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
       float beta = 0.f;
       if (it > 1) {
         double tot[2];
-        cloth_totals(A, inst, 1, 2, sh, tot);
+        cloth_totals<kPersistThreads>(A, inst, 1, 2, sh, tot);
         if (tot[1] <= (double)eta * (double)eta * St.rr_in0 || it - 1 >= cap) {
           if (owner && threadIdx.x == 0) {
             St.istop = 1;
@@ -381,7 +383,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
         continue;
       }
       double tot[1];
-      cloth_totals(A, inst, 0, 1, sh, tot);
+      cloth_totals<kPersistThreads>(A, inst, 0, 1, sh, tot);
       const float alpha = (float)(St.rzh[it & 1] / tot[0]);
       const int lo = max(s0, A.slice_lo[inst]), hi = min(s1, A.slice_hi[inst]);
       for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
@@ -600,25 +602,37 @@ void launch_mx_inner_iteration(const Arena& A, int it, float eta, int cap, cudaS
   g_launches += 3;
 }
 
-void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, cudaStream_t s) {
+template <int T>
+static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm, cudaStream_t s) {
+  int dev = 0, sms = 0, occ = 0;
+  launch_check(cudaGetDevice(&dev), "cudaGetDevice");
+  launch_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+  launch_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mx_persist<T>, T, 0),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+  if (blocks_per_sm > 0) occ = std::min(occ, blocks_per_sm);
+  // at least one slice per warp
+  const int grid = std::max(1, std::min((A.nslice + T / 32 - 1) / (T / 32), sms * std::max(occ, 1)));
+  void* args[] = {(void*)&A, (void*)&eta, (void*)&cap};
+  prof_begin(PK_MX_PERSIST, s);
+  launch_check(cudaLaunchCooperativeKernel((const void*)k_mx_persist<T>, dim3(grid), dim3(T), args, 0, s),
+               "cudaLaunchCooperativeKernel");
+  prof_end(PK_MX_PERSIST, s);
+  g_launches += 1;
+}
+
+void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, int threads,
+                                cudaStream_t s) {
   launch_check(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s), "cudaMemsetAsync");
   const int blocks = (A.nslice * 32 + kSliceThreads - 1) / kSliceThreads;
   k_mx_inner_init<<<blocks, kSliceThreads, 0, s>>>(A);
   k_mx_pstart<<<(A.ni * 32 + 127) / 128, 128, 0, s>>>(A);
   g_launches += 2;
-  int dev = 0, sms = 0, occ = 0;
-  launch_check(cudaGetDevice(&dev), "cudaGetDevice");
-  launch_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-  launch_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mx_persist, kPersistThreads, 0),
-               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-  if (blocks_per_sm > 0) occ = std::min(occ, blocks_per_sm);
-  // at least one slice per warp
-  const int grid = std::max(1, std::min((A.nslice + kPersistWarps - 1) / kPersistWarps, sms * std::max(occ, 1)));
-  void* args[] = {(void*)&A, (void*)&eta, (void*)&cap};
-  prof_begin(PK_MX_PERSIST, s);
-  launch_check(cudaLaunchCooperativeKernel((const void*)k_mx_persist, dim3(grid), dim3(kPersistThreads), args, 0, s), "cudaLaunchCooperativeKernel");
-  prof_end(PK_MX_PERSIST, s);
-  g_launches += 1;
+  if (threads == 1024)
+    persist_launch<1024>(A, eta, cap, blocks_per_sm, s);
+  else if (threads == 512)
+    persist_launch<512>(A, eta, cap, blocks_per_sm, s);
+  else
+    persist_launch<256>(A, eta, cap, blocks_per_sm, s);
 }
 
 void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s) {
