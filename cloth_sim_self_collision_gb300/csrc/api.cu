@@ -382,6 +382,7 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
       A.slice_pbytes = m.upload(pb, s);
 
       A.p32b = m.alloc<float>(3 * (size_t)NV);
+      A.dg_range = m.alloc<unsigned>(2 * (size_t)std::max(ni, 1));
       A.grid_bar = m.alloc<unsigned int>(4);
       CK(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s));
     }

@@ -54,7 +54,8 @@ struct InstState {
   // phase A when the cloth converges and copied to idone in phase B, so each
   // phase's skip test reads a flag that no block changes during that phase
   double rzh[2];
-  int istop, ipad;
+  int istop;
+  int bjac;          // the inner solve applies block-Jacobi (else no preconditioner)
 };
 
 struct Arena {
@@ -125,6 +126,9 @@ struct Arena {
   // and the grid barrier state
   long long* slice_pbytes = nullptr;
   float* p32b = nullptr;
+  // per cloth: smallest and largest diagonal entry of the assembled matrix (as
+  // the bits of positive floats) for the choice of preconditioner
+  unsigned* dg_range = nullptr;
   unsigned int* grid_bar = nullptr; // [0] arrivals, [1] generation, [2] gave up, [3] cloths still iterating
 };
 

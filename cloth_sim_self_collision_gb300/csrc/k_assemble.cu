@@ -157,6 +157,13 @@ __global__ void k_slot_reduce(Arena A) {
     float* dst = A.val32 + A.sell_pos[s];
 #pragma unroll
     for (int k = 0; k < 9; k++) dst[32 * k] = (float)acc[k];
+    if (!fixed) {  // the cloth's range of diagonal entries (positive floats order as their bits)
+      const float lo = (float)fmin(fabs(acc[0]), fmin(fabs(acc[4]), fabs(acc[8])));
+      const float hi = (float)fmax(fabs(acc[0]), fmax(fabs(acc[4]), fabs(acc[8])));
+      const int inst = A.vinst[v];
+      atomicMin(&A.dg_range[2 * inst], __float_as_uint(lo));
+      atomicMax(&A.dg_range[2 * inst + 1], __float_as_uint(hi));
+    }
     // block-Jacobi preconditioner: inverse of the diagonal block (identity if singular)
     const double det = acc[0] * (acc[4] * acc[8] - acc[5] * acc[7]) - acc[1] * (acc[3] * acc[8] - acc[5] * acc[6]) +
                        acc[2] * (acc[3] * acc[7] - acc[4] * acc[6]);
@@ -177,6 +184,11 @@ __global__ void k_slot_reduce(Arena A) {
       for (int k = 0; k < 9; k++) D[k] = (k % 4 == 0) ? 1.f : 0.f;
     }
   }
+}
+
+__global__ void k_dg_reset_hi(Arena A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A.ni) A.dg_range[2 * i + 1] = 0u;
 }
 
 // ordered gradient sum of vertex v: triangles, stencils (then caller's terms)
@@ -373,6 +385,12 @@ void launch_elements(const Arena& A, bool hess, bool masked, cudaStream_t s) {
 }
 
 void launch_slot_reduce(const Arena& A, cudaStream_t s) {
+  if (A.mixed) {
+    // smallest entry starts at a large positive float (0x7f7f7f7f), largest at 0
+    cudaMemsetAsync(A.dg_range, 0x7f, 2 * sizeof(unsigned) * (size_t)A.ni, s);
+    k_dg_reset_hi<<<blocks_for(A.ni), kThreads, 0, s>>>(A);
+    g_launches++;
+  }
   prof_begin(PK_SLOT_REDUCE, s);
   k_slot_reduce<<<blocks_for(A.nb + A.nv), kThreads, 0, s>>>(A);
   prof_end(PK_SLOT_REDUCE, s);
