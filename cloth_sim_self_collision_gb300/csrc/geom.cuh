@@ -311,10 +311,10 @@ CS_HD bool ee_proximity(int i0, int i1, int j0, int j1, V3<double> p0, V3<double
   return true;
 }
 
-// Conservative FP32 rejection for ee_proximity (edges p = a0 a1, q = b0 b1).
-// Each argument points at a vertex's FP32 bounds (lo[3], hi[3]) around its
-// FP64 position.  Returns true only when the FP64 test certainly rejects the
-// pair.  The FP64 test accepts only with rp, rq in [0, 1] and |pm - qm| <=
+// Conservative FP32 rejection for ee_proximity (edges p = p0 p1, q = q0 q1),
+// from vp = p1 - p0, vq = q1 - q0, w = q0 - p0 in FP32 whose components are
+// within E of the exact differences.  Returns true only when the FP64 test
+// certainly rejects the pair.  The FP64 test accepts only with rp, rq in [0, 1] and |pm - qm| <=
 // delta for the points pm, qm at those ratios, which lie on the segments: so
 // any axis along which the two segments are more than delta apart rejects (the
 // edge directions vp and vq, and the common normal vp x vq), in either branch
@@ -324,24 +324,9 @@ CS_HD bool ee_proximity(int i0, int i1, int j0, int j1, V3<double> p0, V3<double
 // within one ulp of the FP64 position, then each product and sum rounded
 // separately); decisions need twice that bound as margin, which also covers
 // the rounding of the FP64 evaluation.
-__device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1, const float* b0, const float* b1,
-                                                float delta_hi) {
+__device__ __forceinline__ bool ee_reject_core(const float* vp, const float* vq, const float* w, float E,
+                                               float delta_hi) {
   const float u = 5.9604645e-8f;  // 2^-24
-  float X = 0.f;
-#pragma unroll
-  for (int k = 0; k < 6; k++)
-    X = fmaxf(X, fmaxf(fmaxf(fabsf(a0[k]), fabsf(a1[k])), fmaxf(fabsf(b0[k]), fabsf(b1[k]))));
-  float vp[3], vq[3], w[3], D = 0.f;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    vp[k] = a1[k] - a0[k];
-    vq[k] = b1[k] - b0[k];
-    w[k] = b0[k] - a0[k];
-    D = fmaxf(D, fmaxf(fabsf(vp[k]), fmaxf(fabsf(vq[k]), fabsf(w[k]))));
-  }
-  // component error of the differences: two coordinates within an ulp each
-  // (ulp <= 2^-23 |x|), plus the rounding of the subtraction
-  const float E = 1.001f * (4.0f * u * X + u * D);
   // t = a . b with its error bound
   auto dot_err = [&](const float* a, const float* b, float& t, float& e) {
     float s = 0.f, l1a = 0.f, l1b = 0.f, sab = 0.f;
@@ -379,28 +364,50 @@ __device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1
     const float gl = g - 2.0f * eg;
     if (gl > 0.f && gl * gl > d2 * (t1 + 2.0f * e1)) return true;
   }
-  const float det = t0 * t1 - t2 * t2;
-  const float edet = 1.001f * (A0 * e1 + A1 * e0 + 2.0f * A2 * e2 + 2.1f * u * (A0 * A1 + A2 * A2) + u * fabsf(det));
-  const float np = t1 * t3 - t2 * t4;
-  const float enp = 1.001f * (A1 * e3 + A3 * e1 + A2 * e4 + A4 * e2 + 2.1f * u * (A1 * A3 + A2 * A4) + u * fabsf(np));
-  const float nq = t2 * t3 - t0 * t4;
-  const float enq = 1.001f * (A2 * e3 + A3 * e2 + A0 * e4 + A4 * e0 + 2.1f * u * (A2 * A3 + A0 * A4) + u * fabsf(nq));
-  if (!(det - 2.0f * edet > 0.f)) return false;
-  const float dhi = (det + 2.0f * edet) * 1.000001f;
-  // certainly the non-parallel branch of dist_edge_edge: ratios
-  if (det - 2.0f * edet > 2.0e-20f) {
-    if (np + 2.0f * enp < 0.f || np - 2.0f * enp > dhi) return true;  // rp < 0 or rp > 1
-    if (nq + 2.0f * enq < 0.f || nq - 2.0f * enq > dhi) return true;  // rq < 0 or rq > 1
+  // The reference's ratios are rp = (t1 t3 - t2 t4) / det, rq = (t2 t3 - t0 t4) / det
+  // with det = t0 t1 - t2^2.  By the Binet-Cauchy identity these equal
+  // n.(w x vq) / |n|^2 and n.(w x vp) / |n|^2 with n = vp x vq, which stay well
+  // conditioned for nearly parallel edges, where t0 t1 - t2^2 cancels.
+  float n[3], en[3], mp[3], emp[3], mq[3], emq[3];
+  auto cross_err = [&](const float* a, const float* b, float* c, float* ec) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int i = (k + 1) % 3, j = (k + 2) % 3;
+      c[k] = a[i] * b[j] - a[j] * b[i];
+      ec[k] = 1.001f * (E * (fabsf(a[i]) + fabsf(b[j]) + fabsf(a[j]) + fabsf(b[i])) + 2.0f * E * E +
+                        2.1f * u * (fabsf(a[i] * b[j]) + fabsf(a[j] * b[i])));
+    }
+  };
+  auto dot3_err = [&](const float* a, const float* ea, const float* b, const float* eb, float& t, float& e) {
+    float s = 0.f, r = 0.f, m = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      s = s + a[k] * b[k];
+      r += (fabsf(a[k]) + ea[k]) * eb[k] + fabsf(b[k]) * ea[k];
+      m += fabsf(a[k] * b[k]);
+    }
+    t = s;
+    e = 1.001f * (r + 3.1f * u * m);
+  };
+  cross_err(vp, vq, n, en);
+  cross_err(w, vq, mp, emp);
+  cross_err(w, vp, mq, emq);
+  float det, edet, np, enp, nq, enq;
+  dot3_err(n, en, n, en, det, edet);
+  dot3_err(n, en, mp, emp, np, enp);
+  dot3_err(n, en, mq, emq, nq, enq);
+  // the reference evaluates the t-formulas in FP64: their rounding (inputs, the
+  // five dot products, products and differences) stays below these bounds
+  const float e64 = 2.0e-15f;
+  const float fdet = e64 * (A0 * A1 + A2 * A2), fnp = e64 * (A1 * A3 + A2 * A4), fnq = e64 * (A2 * A3 + A0 * A4);
+  if (!(det - 2.0f * edet - fdet > 0.f)) return false;
+  const float dhi = (det + 2.0f * edet + fdet) * 1.000001f;
+  // certainly the non-parallel branch of dist_edge_edge (|vp x vq| > 1e-10): ratios
+  if (det - 2.0f * edet - fdet > 2.0e-20f) {
+    if (np + 2.0f * enp + fnp < 0.f || np - 2.0f * enp - fnp > dhi) return true;  // rp < 0 or rp > 1
+    if (nq + 2.0f * enq + fnq < 0.f || nq - 2.0f * enq - fnq > dhi) return true;  // rq < 0 or rq > 1
   }
   // axis n = vp x vq (|n|^2 = det): both segments project to single points
-  float n[3], en[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int i = (k + 1) % 3, j = (k + 2) % 3;
-    n[k] = vp[i] * vq[j] - vp[j] * vq[i];
-    en[k] = 1.001f * (E * (fabsf(vp[i]) + fabsf(vq[j]) + fabsf(vp[j]) + fabsf(vq[i])) + 2.0f * E * E +
-                      2.1f * u * (fabsf(vp[i] * vq[j]) + fabsf(vp[j] * vq[i])));
-  }
   float s = 0.f, es = 0.f;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -410,6 +417,41 @@ __device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1
   es *= 1.001f;
   const float sl = fabsf(s) - 2.0f * es;
   return sl > 0.f && sl * sl > d2 * dhi;
+}
+
+// The filter on the FP32 vertex bounds (lo[3], hi[3] around each FP64 position,
+// so every coordinate is within one ulp of it): absolute errors of 2^-23 |x|.
+__device__ __forceinline__ bool ee_prx_reject32(const float* a0, const float* a1, const float* b0, const float* b1,
+                                                float delta_hi) {
+  const float u = 5.9604645e-8f;  // 2^-24
+  float X = 0.f;
+#pragma unroll
+  for (int k = 0; k < 6; k++)
+    X = fmaxf(X, fmaxf(fmaxf(fabsf(a0[k]), fabsf(a1[k])), fmaxf(fabsf(b0[k]), fabsf(b1[k]))));
+  float vp[3], vq[3], w[3], D = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    vp[k] = a1[k] - a0[k];
+    vq[k] = b1[k] - b0[k];
+    w[k] = b0[k] - a0[k];
+    D = fmaxf(D, fmaxf(fabsf(vp[k]), fmaxf(fabsf(vq[k]), fabsf(w[k]))));
+  }
+  // two coordinates within an ulp each (ulp <= 2^-23 |x|), plus the subtraction
+  return ee_reject_core(vp, vq, w, 1.001f * (4.0f * u * X + u * D), delta_hi);
+}
+
+// The filter on differences taken in FP64 and rounded to FP32: relative errors
+// of 2^-24 (plus the FP64 subtraction's), which resolves nearly parallel edges
+// whose angle the absolute FP32 coordinates cannot.
+__device__ __forceinline__ bool ee_prx_reject_rel(V3<double> p0, V3<double> p1, V3<double> q0, V3<double> q1,
+                                                  float delta_hi) {
+  const float vp[3] = {(float)(p1.x - p0.x), (float)(p1.y - p0.y), (float)(p1.z - p0.z)};
+  const float vq[3] = {(float)(q1.x - q0.x), (float)(q1.y - q0.y), (float)(q1.z - q0.z)};
+  const float w[3] = {(float)(q0.x - p0.x), (float)(q0.y - p0.y), (float)(q0.z - p0.z)};
+  float D = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) D = fmaxf(D, fmaxf(fabsf(vp[k]), fmaxf(fabsf(vq[k]), fabsf(w[k]))));
+  return ee_reject_core(vp, vq, w, 1.001f * (5.9604645e-8f + 2.0e-16f) * D, delta_hi);
 }
 
 CS_HD bool fv_ccd(int i0, int i1, int i2, int i3, V3<double> p0, V3<double> p1, V3<double> p2, V3<double> p3,

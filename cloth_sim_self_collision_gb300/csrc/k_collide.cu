@@ -424,11 +424,14 @@ __global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, c
     const int k = test - 6;
     const int i0 = A.tri[3 * ta + kEE[k][0]], i1 = A.tri[3 * ta + kEE[k][1]];
     const int j0 = A.tri[3 * tb + kEE[k][2]], j1 = A.tri[3 * tb + kEE[k][3]];
-    count_fp64_test(A, ccd ? 5 : 3);
     const V3<double> p0 = ld3(xs, i0), p1 = ld3(xs, i1), q0 = ld3(xs, j0), q1 = ld3(xs, j1);
     if (!ccd) {
+      // second filter stage on FP64 differences (nearly parallel edges)
+      if (ee_prx_reject_rel(p0, p1, q0, q1, __double2float_ru(delta))) continue;
+      count_fp64_test(A, 3);
       if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
     } else {
+      count_fp64_test(A, 5);
       if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, end_pos(xs, vs, i0, P.dt), end_pos(xs, vs, i1, P.dt),
                  end_pos(xs, vs, j0, P.dt), end_pos(xs, vs, j1, P.dt)))
         emit(C, 0, i0, i1, j0, j1, na, nb, test);
