@@ -274,6 +274,95 @@ CS_HD double coplanar_time(V3<double> s0, V3<double> s1, V3<double> s2, V3<doubl
   return bisect_cubic(r0, r1, f0, k0, k1, k2, k3);
 }
 
+// FP32 vector with a bound on each component's error
+struct F3E {
+  float v[3], e[3];
+};
+
+__device__ __forceinline__ F3E f3e_cross(const F3E& a, const F3E& b) {
+  const float u = 5.9604645e-8f;
+  F3E c;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int i = (k + 1) % 3, j = (k + 2) % 3;
+    const float m1 = a.v[i] * b.v[j], m2 = a.v[j] * b.v[i];
+    c.v[k] = m1 - m2;
+    c.e[k] = 1.001f * ((fabsf(a.v[i]) + a.e[i]) * b.e[j] + fabsf(b.v[j]) * a.e[i] +
+                       (fabsf(a.v[j]) + a.e[j]) * b.e[i] + fabsf(b.v[i]) * a.e[j] +
+                       2.1f * u * (fabsf(m1) + fabsf(m2)));
+  }
+  return c;
+}
+
+// a . (b x c) with its error bound and the sum of the magnitudes of its terms
+__device__ __forceinline__ void f3e_stp(const F3E& a, const F3E& b, const F3E& c, float& t, float& e, float& m) {
+  const float u = 5.9604645e-8f;
+  const F3E x = f3e_cross(b, c);
+  float s = 0.f, r = 0.f, mm = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float p = a.v[k] * x.v[k];
+    s = s + p;
+    r += (fabsf(a.v[k]) + a.e[k]) * x.e[k] + fabsf(x.v[k]) * a.e[k];
+    mm += fabsf(a.v[k]) * (fabsf(b.v[(k + 1) % 3] * c.v[(k + 2) % 3]) + fabsf(b.v[(k + 2) % 3] * c.v[(k + 1) % 3]));
+  }
+  t = s;
+  e = 1.001f * (r + 3.1f * u * mm);
+  m = mm;
+}
+
+__device__ __forceinline__ F3E f3e_round(V3<double> d) {
+  F3E r;
+  r.v[0] = (float)d.x;
+  r.v[1] = (float)d.y;
+  r.v[2] = (float)d.z;
+#pragma unroll
+  for (int k = 0; k < 3; k++) r.e[k] = 5.97e-8f * fabsf(r.v[k]);  // round to nearest: 2^-24 relative
+  return r;
+}
+
+// True when FindCoplanerInterp (coplanar_time) certainly returns -1 for the
+// vectors it forms from the start positions and displacements: x_i = s_i - s0,
+// v_i = (e_i - e0) - x_i, computed in FP64 exactly as it does and passed here.
+// The cubic k0 + k1 t + k2 t^2 + k3 t^3 (k from the triple products) has its
+// Bernstein coefficients on [0, 1] evaluated in FP32 with error bounds; when
+// all four keep one sign with twice their bound to spare (which also covers the
+// FP64 rounding of the coefficients and of the cubic's evaluations), the cubic
+// keeps that sign on [0, 1], no evaluation the root finder makes changes sign,
+// and it returns -1.
+__device__ __forceinline__ bool ccd_no_root32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<double> v1d,
+                                              V3<double> v2d, V3<double> v3d) {
+  const float u = 5.9604645e-8f;
+  const F3E x1 = f3e_round(x1d), x2 = f3e_round(x2d), x3 = f3e_round(x3d);
+  const F3E v1 = f3e_round(v1d), v2 = f3e_round(v2d), v3 = f3e_round(v3d);
+  float t[8], e[8], m[8];
+  f3e_stp(x3, x1, x2, t[0], e[0], m[0]);  // k0
+  f3e_stp(v3, x1, x2, t[1], e[1], m[1]);  // k1
+  f3e_stp(x3, v1, x2, t[2], e[2], m[2]);
+  f3e_stp(x3, x1, v2, t[3], e[3], m[3]);
+  f3e_stp(v3, v1, x2, t[4], e[4], m[4]);  // k2
+  f3e_stp(v3, x1, v2, t[5], e[5], m[5]);
+  f3e_stp(x3, v1, v2, t[6], e[6], m[6]);
+  f3e_stp(v3, v1, v2, t[7], e[7], m[7]);  // k3
+  const float k0 = t[0], k1 = (t[1] + t[2]) + t[3], k2 = (t[4] + t[5]) + t[6], k3 = t[7];
+  const float mk = m[0] + m[1] + m[2] + m[3] + m[4] + m[5] + m[6] + m[7];
+  const float ek0 = e[0], ek1 = 1.001f * (e[1] + e[2] + e[3] + 2.1f * u * (fabsf(t[1]) + fabsf(t[2]) + fabsf(t[3]))),
+              ek2 = 1.001f * (e[4] + e[5] + e[6] + 2.1f * u * (fabsf(t[4]) + fabsf(t[5]) + fabsf(t[6]))),
+              ek3 = e[7];
+  // FP64 rounding of the reference's coefficients and cubic evaluations
+  const float f64 = 4.0e-15f * mk;
+  // Bernstein coefficients of the cubic on [0, 1]
+  const float b0 = k0, b1 = k0 + k1 * (1.0f / 3.0f), b2 = k0 + k1 * (2.0f / 3.0f) + k2 * (1.0f / 3.0f),
+              b3 = ((k0 + k1) + k2) + k3;
+  const float eb0 = ek0, eb1 = 1.001f * (ek0 + ek1 * 0.34f + 2.0f * u * (fabsf(k0) + fabsf(k1))),
+              eb2 = 1.001f * (ek0 + ek1 * 0.67f + ek2 * 0.34f + 3.0f * u * (fabsf(k0) + fabsf(k1) + fabsf(k2))),
+              eb3 = 1.001f * (ek0 + ek1 + ek2 + ek3 + 3.1f * u * (fabsf(k0) + fabsf(k1) + fabsf(k2) + fabsf(k3)));
+  const bool pos = b0 - 2.0f * eb0 > f64 && b1 - 2.0f * eb1 > f64 && b2 - 2.0f * eb2 > f64 && b3 - 2.0f * eb3 > f64;
+  const bool neg = b0 + 2.0f * eb0 < -f64 && b1 + 2.0f * eb1 < -f64 && b2 + 2.0f * eb2 < -f64 &&
+                   b3 + 2.0f * eb3 < -f64;
+  return pos || neg;
+}
+
 // ---------------------------------------------------------------------------
 // elementary contact tests (bvh_aabb.cpp:392-438, 666-793)
 // ---------------------------------------------------------------------------

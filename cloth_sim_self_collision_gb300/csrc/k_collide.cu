@@ -319,7 +319,11 @@ __device__ __forceinline__ void enqueue(const ContactBufs& C, int kind, int pid,
   C.queue[kind][slot] = make_int2(pid, test);
 }
 
-__global__ void k_narrow_filter(Arena A, ContactBufs C, int ccd, double delta_override, int npairs) {
+__global__ void __launch_bounds__(kT) k_narrow_filter(Arena A, ContactBufs C, int ccd, double delta_override,
+                                                      int npairs) {
+  // the 9 edge pairs of a triangle pair (kEE), as compile-time indices
+  constexpr int kE[9][4] = {{0, 1, 0, 1}, {0, 1, 1, 2}, {0, 1, 2, 0}, {1, 2, 0, 1}, {1, 2, 1, 2},
+                            {1, 2, 2, 0}, {2, 0, 0, 1}, {2, 0, 1, 2}, {2, 0, 2, 0}};
   const int pid = blockIdx.x * blockDim.x + threadIdx.x;
   if (pid >= npairs) return;
   const int2 pr = C.pairs[pid];
@@ -329,31 +333,60 @@ __global__ void k_narrow_filter(Arena A, ContactBufs C, int ccd, double delta_ov
   if (A.st[inst].diverged) return;
   const double delta = delta_override >= 0 ? delta_override : A.prm[inst].contact_clearance;
   const float du = __double2float_ru(delta);
-  const int va[3] = {A.tri[3 * ta], A.tri[3 * ta + 1], A.tri[3 * ta + 2]};
-  const int vb[3] = {A.tri[3 * tb], A.tri[3 * tb + 1], A.tri[3 * tb + 2]};
+  int va[3], vb[3];
+  // the FP32 bounds (lo[3], hi[3]) of the six vertices, read once
+  float ba[3][6], bb[3][6];
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    va[m] = A.tri[3 * ta + m];
+    vb[m] = A.tri[3 * tb + m];
+    const float2* pa = reinterpret_cast<const float2*>(A.vb32 + 6 * (size_t)va[m]);
+    const float2* pb = reinterpret_cast<const float2*>(A.vb32 + 6 * (size_t)vb[m]);
+#pragma unroll
+    for (int h = 0; h < 3; h++) {
+      const float2 x = pa[h], y = pb[h];
+      ba[m][2 * h] = x.x;
+      ba[m][2 * h + 1] = x.y;
+      bb[m][2 * h] = y.x;
+      bb[m][2 * h + 1] = y.y;
+    }
+  }
   // face-vertex: the vertex inside the face's box (the reference's aBB quirk for
   // proximity: the node whose index is the triangle's index within its cloth)
-#pragma unroll 1
-  for (int test = 0; test < 6; test++) {
-    const bool fa = test < 3;
-    const int* f = fa ? va : vb;
-    const int q = fa ? vb[test] : va[test - 3];
-    if (q == f[0] || q == f[1] || q == f[2]) continue;
-    const int tf = fa ? ta : tb;
-    const int bn = ccd ? (fa ? na : nb) : A.noff[inst] + (tf - A.toff[inst]);
-    if (!overlap32(A.box32 + 6 * (size_t)bn, A.vb32 + 6 * (size_t)q)) continue;
-    enqueue(C, 0, pid, test);
+  {
+    float fa[6], fb[6];
+    const int bna = ccd ? na : A.noff[inst] + (ta - A.toff[inst]);
+    const int bnb = ccd ? nb : A.noff[inst] + (tb - A.toff[inst]);
+    const float2* qa = reinterpret_cast<const float2*>(A.box32 + 6 * (size_t)bna);
+    const float2* qb = reinterpret_cast<const float2*>(A.box32 + 6 * (size_t)bnb);
+#pragma unroll
+    for (int h = 0; h < 3; h++) {
+      const float2 x = qa[h], y = qb[h];
+      fa[2 * h] = x.x;
+      fa[2 * h + 1] = x.y;
+      fb[2 * h] = y.x;
+      fb[2 * h + 1] = y.y;
+    }
+#pragma unroll
+    for (int test = 0; test < 6; test++) {
+      const bool on_a = test < 3;
+      const int k = on_a ? test : test - 3;
+      const int q = on_a ? vb[k] : va[k];
+      const int* f = on_a ? va : vb;
+      if (q == f[0] || q == f[1] || q == f[2]) continue;
+      if (!overlap32(on_a ? fa : fb, on_a ? bb[k] : ba[k])) continue;
+      enqueue(C, 0, pid, test);
+    }
   }
-#pragma unroll 1
+#pragma unroll
   for (int k = 0; k < 9; k++) {
-    const int i0 = va[kEE[k][0]], i1 = va[kEE[k][1]];
-    const int j0 = vb[kEE[k][2]], j1 = vb[kEE[k][3]];
+    const int i0 = va[kE[k][0]], i1 = va[kE[k][1]];
+    const int j0 = vb[kE[k][2]], j1 = vb[kE[k][3]];
     if (i0 == j0 || i0 == j1 || i1 == j0 || i1 == j1) continue;
     // for CCD the edges' swept boxes must overlap; for proximity the reference's
     // six slab tests (bvh_aabb.cpp:420-425) are bounded with directed rounding,
     // then the closest-point / distance filter
-    const float *a0 = A.vb32 + 6 * (size_t)i0, *a1 = A.vb32 + 6 * (size_t)i1;
-    const float *b0 = A.vb32 + 6 * (size_t)j0, *b1 = A.vb32 + 6 * (size_t)j1;
+    const float *a0 = ba[kE[k][0]], *a1 = ba[kE[k][1]], *b0 = bb[kE[k][2]], *b1 = bb[kE[k][3]];
     bool keep = true;
     if (ccd) {
       float ea[6], eb[6];
@@ -431,10 +464,16 @@ __global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, c
       count_fp64_test(A, 3);
       if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
     } else {
+      const V3<double> p0e = end_pos(xs, vs, i0, P.dt), p1e = end_pos(xs, vs, i1, P.dt);
+      const V3<double> q0e = end_pos(xs, vs, j0, P.dt), q1e = end_pos(xs, vs, j1, P.dt);
+      {
+        // no coplanarity in [0, 1]: the vectors coplanar_time forms, in FP64 as it does
+        const V3<double> x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0;
+        const V3<double> v1 = (p1e - p0e) - x1, v2 = (q0e - p0e) - x2, v3 = (q1e - p0e) - x3;
+        if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
+      }
       count_fp64_test(A, 5);
-      if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, end_pos(xs, vs, i0, P.dt), end_pos(xs, vs, i1, P.dt),
-                 end_pos(xs, vs, j0, P.dt), end_pos(xs, vs, j1, P.dt)))
-        emit(C, 0, i0, i1, j0, j1, na, nb, test);
+      if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, p0e, p1e, q0e, q1e)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
     }
   }
 }

@@ -11,9 +11,11 @@
 namespace cs {
 
 // Leaf pairs one triangle's broad-phase walk may emit before its cloth is taken
-// as blown up (normal frames stay far below: a few tens per triangle, a few
-// hundred in deep folds).
-constexpr int kMaxPairsPerTriangle = 512;
+// as blown up.  Normal frames stay far below: a few tens per triangle, a few
+// hundred in deep folds or with fast incoherent motion.  A blown-up cloth is
+// normally caught first by its speed (kMaxSpeed); this limit bounds the pair
+// buffers when it is not.
+constexpr int kMaxPairsPerTriangle = 4096;
 // A velocity component above this (m/s) after the implicit step also marks the
 // cloth as blown up (no cloth frame of the reference's scenes comes near it).
 constexpr double kMaxSpeed = 1.0e3;

@@ -31,7 +31,7 @@ extern "C" {
 #define CS_ERR_CAPACITY 5     /* a caller-supplied output buffer is too small        */
 #define CS_ERR_TIMEOUT 6      /* a bounded device wait gave up                        */
 #define CS_ERR_DIVERGED 7     /* a cloth blew up (a speed above 1000 m/s after its implicit
-                                 step, or more than 512 overlapping leaf pairs for one
+                                 step, or more than 4096 overlapping leaf pairs for one
                                  triangle); it is no longer stepped                    */
 
 /* precision of the implicit solve */

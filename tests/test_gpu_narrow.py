@@ -74,3 +74,27 @@ def test_prx_contacts_fold_probe_scaled(ctx, oracle_port):
         assert np.array_equal(a, b), (s, len(a), len(b))
     ctx.remove_cloth(cid)
     orc.close()
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_ccd_contacts_crumpled(ctx, oracle_port, seed):
+    """CCD contact sets on crumpled sheets moving with random velocities of
+    several scales: coplanarity times cross [0, 1] at many pairs, which the FP32
+    no-root certificate in front of the FP64 cubic must never reject."""
+    c = scene.square_cloth(31, 0.5, 0.4, sphere_radius=0.2, clearance=0.01, seed=40 + seed,
+                           solver_kind=scene.SOLVER_CG, tol=1e-6, maxit=1000)
+    cid = ctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    rng = np.random.default_rng(100 + seed)
+    x = crumpled(c, seed, amp_xy=0.003 * (1 + seed), amp_z=0.005 * (1 + seed % 3))
+    total = 0
+    for scale in (0.05, 0.3, 1.0, 3.0):
+        v = rng.normal(0.0, scale, x.size)
+        v[2::3] -= 2.0  # a common downward drift, as when falling
+        a = ctx.contacts_ccd(cid, x, v, c.params.dt, c.params.contact_clearance)
+        b = orc.contacts_ccd(x, v, c.params.dt, c.params.contact_clearance)
+        assert np.array_equal(a, b), (seed, scale, len(a), len(b))
+        total += len(b)
+    ctx.remove_cloth(cid)
+    orc.close()
+    assert total > 0
