@@ -149,6 +149,19 @@ __device__ __forceinline__ int warp_append(int* counter) {
 // kMaxPairsPerTriangle leaves to its right marks its cloth as blown up (the
 // reference would go on with a quadratic contact set); the cloth's pairs are
 // then dropped by the narrow phase and the host stops stepping it.
+// Nodes are culled with the outward-rounded FP32 boxes (a miss there is a
+// miss in FP64; a node's box holds its children's), and each leaf pair is
+// accepted by the FP64 boxes, so the pairs are exactly the reference's.
+__device__ __forceinline__ void load_box32(const float* src, float* b) {
+  const float2* p = reinterpret_cast<const float2*>(src);
+#pragma unroll
+  for (int h = 0; h < 3; h++) {
+    const float2 v = p[h];
+    b[2 * h] = v.x;
+    b[2 * h + 1] = v.y;
+  }
+}
+
 __global__ void k_traverse(Arena A, ContactBufs C) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nt) return;
@@ -157,16 +170,24 @@ __global__ void k_traverse(Arena A, ContactBufs C) {
   const int la = A.tri_leaf[t];
   const int oa = A.leaf_lo[la];
   const Box ba = A.box[la];
+  float ba32[6];
+  load_box32(A.box32 + 6 * (size_t)la, ba32);
   int k = A.preoff[inst];
   const int end = A.preoff[inst + 1];
   int found = 0;
   while (k < end) {
     const int n = A.pre[k];
-    if (A.leaf_hi[n] <= oa || !box_overlap(ba, A.box[n])) {
+    float nb32[6];
+    load_box32(A.box32 + 6 * (size_t)n, nb32);
+    if (A.leaf_hi[n] <= oa || !overlap32(ba32, nb32)) {
       k = A.skip[k];
       continue;
     }
     if (A.node[3 * n + 2] == -1) {
+      if (!box_overlap(ba, A.box[n])) {
+        k = A.skip[k];
+        continue;
+      }
       if (++found > kMaxPairsPerTriangle) {
         A.st[inst].diverged = 1;
         return;
@@ -194,16 +215,24 @@ __global__ void k_traverse_dirty(Arena A, ContactBufs C) {
   const int la = A.tri_leaf[t];
   const int oa = A.leaf_lo[la];
   const Box ba = A.box[la];
+  float ba32[6];
+  load_box32(A.box32 + 6 * (size_t)la, ba32);
   int k = A.preoff[inst];
   const int end = A.preoff[inst + 1];
   int found = 0;
   while (k < end) {
     const int n = A.pre[k];
-    if (!box_overlap(ba, A.box[n])) {
+    float nb32[6];
+    load_box32(A.box32 + 6 * (size_t)n, nb32);
+    if (!overlap32(ba32, nb32)) {
       k = A.skip[k];
       continue;
     }
     if (A.node[3 * n + 2] == -1) {
+      if (!box_overlap(ba, A.box[n])) {
+        k = A.skip[k];
+        continue;
+      }
       if (++found > 2 * kMaxPairsPerTriangle) {
         A.st[inst].diverged = 1;
         return;
