@@ -50,12 +50,13 @@ struct InstState {
   int total_iters;   // inner iterations summed over refinement cycles
   int cycles;        // refinement cycles
   double red[3];     // per-cloth totals of the slice partials: p.q, r.z, r.r
-  // persistent inner solve: r.z of the iterations by parity; istop is set in
-  // phase A when the cloth converges and copied to idone in phase B, so each
-  // phase's skip test reads a flag that no block changes during that phase
+  // persistent inner solve: r.z of the iterations by parity; istop is set at
+  // the end of phase B when the cloth converges (no block reads it before the
+  // barrier that follows); alpha and beta as the cloth's last block left them
   double rzh[2];
   int istop;
   int bjac;          // the inner solve applies block-Jacobi (else no preconditioner)
+  float alpha32, beta32;
 };
 
 struct Arena {

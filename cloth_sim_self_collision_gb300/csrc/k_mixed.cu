@@ -239,27 +239,27 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
 
 // ---- persistent inner solve ---------------------------------------------------------
 // One cooperative launch runs every inner CG iteration of a refinement cycle for
-// all cloths.  Each block owns a contiguous range of slices (and so touches one
-// or a few cloths); its warps take the range's slices in turn.  Per iteration,
-// two phases separated by grid barriers:
-//   A: from the r.z and r.r slice partials of the previous phase B, every block
-//      touching a cloth computes the cloth's totals itself (a fixed-order block
-//      sum over all its slices) and decides convergence (|r|^2 <= eta^2 |r0|^2,
-//      or the cap) or beta; then p = z + beta p_prev is built on the fly (for
-//      the rows a slice reads and for its own rows, which it stores),
-//      q = A32 p, and the slice partials of p.q are written.
-//   B: from the p.q partials, alpha = r.z / p.q per cloth (again computed by
-//      every block that needs it), then d += alpha p, r -= alpha q,
-//      z = D^-1 r, and the slice partials of r.z and r.r.
-// The block holding a cloth's first slice records its convergence (istop in
-// phase A, copied to idone in phase B, so that each phase's skip test reads a
-// flag no block changes during that phase) and decrements the count of cloths
-// still iterating; every block reads that count
-// right after the barrier that follows phase A (nothing changes it before the
-// next phase A), so all blocks leave the loop together.  The direction buffers
-// alternate between iterations.  Totals are the same fixed-order sums in every
-// block: results depend neither on the launch shape nor on the other cloths.
+// all cloths.  Per iteration, two phases separated by grid barriers:
+//   A: p = z + beta p_prev is built on the fly (for the rows a slice reads and
+//      for its own rows, which it stores), q = A32 p, and the slice partials
+//      of p.q; the last block to finish a cloth's slices sums its partials and
+//      stores alpha = r.z / p.q.
+//   B: d += alpha p, r -= alpha q, z = D^-1 r, and the slice partials of r.z
+//      and r.r; the last block to finish a cloth's slices sums them and decides
+//      convergence (|r|^2 <= eta^2 |r0|^2, or the cap) or stores beta.
+// "Last block" is a per-cloth ticket counted in slices, so each total is
+// summed once, in slice order by a block of fixed size: results depend neither
+// on the launch shape nor on the other cloths.  A converged cloth sets istop and
+// decrements the count of cloths still iterating; all blocks read that count
+// after the barrier that ends phase B (nothing changes it before the next
+// phase B), so they leave the loop together.
+// Work split: the slices of the cloths still iterating, in arena order, are cut
+// into one contiguous range per block, re-cut whenever a cloth stops, so blocks
+// do not idle on converged cloths (arenas of more than kRebalanceMax cloths
+// keep the static cut over all slices and skip converged cloths).  The
+// direction buffers alternate between iterations.
 constexpr unsigned kSpinLimit = 1u << 22;  // ~1 s of polling at the least
+constexpr int kRebalanceMax = 2048;        // cloths whose slice prefix fits in shared memory
 
 // Grid-wide barrier on A.grid_bar with a bounded wait.  Returns false when the
 // wait ran out here or in another block (the flag A.grid_bar[2] is then set and
@@ -312,46 +312,137 @@ __device__ void cloth_totals(const Arena& A, int inst, int f0, int nf, double* s
   }
 }
 
+// After a block's n slices of cloth inst have written their partials: true in
+// the block whose slices complete the cloth (it then resets the ticket).
+__device__ bool last_portion(const Arena& A, int inst, int n, int* s_flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int total = A.slice_hi[inst] - A.slice_lo[inst];
+    const int old = atomicAdd(&A.red_cnt[inst], n);
+    const int last = old + n == total;
+    if (last) {
+      A.red_cnt[inst] = 0;
+      __threadfence();
+    }
+    *s_flag = last;
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+__device__ __forceinline__ bool iterating(const Arena& A, int inst) {
+  return A.active[inst] && !A.st[inst].done && !A.st[inst].istop;
+}
+
+// This block's share of the slices of the cloths still iterating: cloths
+// [c0, c1], clipped to [a0, a1) in the prefix s_pref (compact cut) or to the
+// slices [a0, a1) themselves (static cut).
+struct PersistRange {
+  int a0, a1, c0, c1;
+};
+
 template <int kPersistThreads>
-__global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float eta, int cap) {
+__device__ void compact_range(const Arena& A, int* s_pref, int* s_wsum, PersistRange& R) {
+  constexpr int kPersistWarps = kPersistThreads / 32;
+  const int ni = A.ni;
+  const int per = (ni + kPersistThreads - 1) / kPersistThreads;
+  const int b0 = min(ni, threadIdx.x * per), b1 = min(ni, b0 + per);
+  int sum = 0;
+  for (int c = b0; c < b1; c++) sum += iterating(A, c) ? A.slice_hi[c] - A.slice_lo[c] : 0;
+  // exclusive block scan of the thread sums
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  __syncthreads();
+  if (lane == 31) s_wsum[warp] = inc;
+  __syncthreads();
+  int off = inc - sum;
+  for (int w = 0; w < warp; w++) off += s_wsum[w];
+  for (int c = b0; c < b1; c++) {
+    s_pref[c] = off;
+    off += iterating(A, c) ? A.slice_hi[c] - A.slice_lo[c] : 0;
+  }
+  if (threadIdx.x == kPersistThreads - 1) s_pref[ni] = off;
+  __syncthreads();
+  (void)kPersistWarps;
+  const long long total = s_pref[ni];
+  R.a0 = (int)(total * blockIdx.x / gridDim.x);
+  R.a1 = (int)(total * (blockIdx.x + 1) / gridDim.x);
+  // the largest c with s_pref[c] <= x
+  auto find = [&](int x) {
+    int lo = 0, hi = ni - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_pref[mid] <= x) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  };
+  if (R.a0 < R.a1) {
+    R.c0 = find(R.a0);
+    R.c1 = find(R.a1 - 1);
+  } else {
+    R.c0 = 0;
+    R.c1 = -1;
+  }
+}
+
+// slices [lo, hi) of cloth inst in this block's range; false when empty
+__device__ __forceinline__ bool portion(const Arena& A, const PersistRange& R, bool compact, const int* s_pref,
+                                        int inst, int& lo, int& hi) {
+  if (compact) {
+    const int p0 = s_pref[inst];
+    lo = A.slice_lo[inst] + (max(R.a0, p0) - p0);
+    hi = A.slice_lo[inst] + (min(R.a1, s_pref[inst + 1]) - p0);
+  } else {
+    if (!iterating(A, inst)) return false;
+    lo = max(R.a0, A.slice_lo[inst]);
+    hi = min(R.a1, A.slice_hi[inst]);
+  }
+  return lo < hi;
+}
+
+template <int kPersistThreads>
+__global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads) k_mx_persist(Arena A, float eta, int cap) {
   constexpr int kPersistWarps = kPersistThreads / 32;
   __shared__ double sh[kPersistWarps];
-  __shared__ int s_left;
+  __shared__ int s_wsum[kPersistWarps];
+  __shared__ int s_flag, s_left;
+  __shared__ int s_pref[kRebalanceMax + 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // this block's slices [s0, s1)
-  const long long S = A.nslice;
-  const int s0 = (int)(S * blockIdx.x / gridDim.x), s1 = (int)(S * (blockIdx.x + 1) / gridDim.x);
-  const int c0 = s0 < s1 ? A.slice_inst[s0] : 0, c1 = s0 < s1 ? A.slice_inst[s1 - 1] : -1;
-  for (int it = 1; it <= cap + 1; it++) {
+  const bool compact = A.ni <= kRebalanceMax;
+  PersistRange R;
+  {
+    const long long S = A.nslice;
+    R.a0 = (int)(S * blockIdx.x / gridDim.x);
+    R.a1 = (int)(S * (blockIdx.x + 1) / gridDim.x);
+    R.c0 = R.a0 < R.a1 ? A.slice_inst[R.a0] : 0;
+    R.c1 = R.a0 < R.a1 ? A.slice_inst[R.a1 - 1] : -1;
+  }
+  if (threadIdx.x == 0) s_left = ((volatile unsigned*)A.grid_bar)[3];
+  __syncthreads();
+  unsigned cut_at = 0xffffffffu;  // cloths iterating when the range was cut
+  for (int it = 1; it <= cap; it++) {
+    const unsigned left = (unsigned)s_left;
+    if (left == 0u) break;
+    if (compact && left != cut_at) {
+      compact_range<kPersistThreads>(A, s_pref, s_wsum, R);
+      cut_at = left;
+    }
     const float* Pold = (it & 1) ? A.p32 : A.p32b;
     float* Pnew = (it & 1) ? A.p32b : A.p32;
-    // ---- phase A: convergence, direction, SpMV
-    for (int inst = c0; inst <= c1; inst++) {
-      if (!A.active[inst]) continue;
-      InstState& St = A.st[inst];
-      if (St.done || St.idone) continue;  // idone changes only in phase B
-      const bool owner = s0 <= A.slice_lo[inst] && A.slice_lo[inst] < s1;
-      float beta = 0.f;
-      if (it > 1) {
-        double tot[2];
-        cloth_totals<kPersistThreads>(A, inst, 1, 2, sh, tot);
-        if (tot[1] <= (double)eta * (double)eta * St.rr_in0 || it - 1 >= cap) {
-          if (owner && threadIdx.x == 0) {
-            St.istop = 1;
-            St.inner_iters = it - 1;
-            St.red[1] = tot[0];
-            St.red[2] = tot[1];
-            atomicSub(&A.grid_bar[3], 1u);
-          }
-          continue;
-        }
-        beta = (float)(tot[0] / St.rzh[(it - 1) & 1]);
-        if (owner && threadIdx.x == 0) {
-          St.rzh[it & 1] = tot[0];
-          St.inner_iters = it - 1;
-        }
-      }
-      const int lo = max(s0, A.slice_lo[inst]), hi = min(s1, A.slice_hi[inst]);
+    // ---- phase A: direction, SpMV, p.q
+    for (int inst = R.c0; inst <= R.c1; inst++) {
+      int lo, hi;
+      if (!portion(A, R, compact, s_pref, inst, lo, hi)) continue;
+      const InstState& St = A.st[inst];
+      const float beta = it > 1 ? St.beta32 : 0.f;
+      const int bjac = St.bjac;
       for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
         const int row = A.slice_row0[sl] + lane;
         const int w = A.slice_w[sl];
@@ -387,28 +478,24 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
           A.part32[3 * sl + 0] = pq;
           if (A.count_bytes) {  // without the preconditioner no D^-1 is read (36 B a row)
             const int rows = min(32, A.voff[inst + 1] - A.slice_row0[sl]);
-            atomicAdd(&A.bytes_acc[6], (unsigned long long)(A.slice_pbytes[sl] - (St.bjac ? 0 : 36LL * rows)));
+            atomicAdd(&A.bytes_acc[6], (unsigned long long)(A.slice_pbytes[sl] - (bjac ? 0 : 36LL * rows)));
           }
         }
       }
+      if (last_portion(A, inst, hi - lo, &s_flag)) {
+        double tot[1];
+        cloth_totals<kPersistThreads>(A, inst, 0, 1, sh, tot);
+        if (threadIdx.x == 0) A.st[inst].alpha32 = (float)(A.st[inst].rzh[it & 1] / tot[0]);
+      }
     }
     if (!grid_sync(A)) return;
-    if (threadIdx.x == 0) s_left = ((volatile unsigned*)A.grid_bar)[3] != 0u;
-    __syncthreads();
-    if (!s_left) break;
-    // ---- phase B: step length and update
-    for (int inst = c0; inst <= c1; inst++) {
-      if (!A.active[inst]) continue;
+    // ---- phase B: update, r.z and r.r, convergence or beta
+    for (int inst = R.c0; inst <= R.c1; inst++) {
+      int lo, hi;
+      if (!portion(A, R, compact, s_pref, inst, lo, hi)) continue;
       InstState& St = A.st[inst];
-      if (St.done) continue;
-      if (St.istop) {  // istop changes only in phase A
-        if (s0 <= A.slice_lo[inst] && A.slice_lo[inst] < s1 && threadIdx.x == 0) St.idone = 1;
-        continue;
-      }
-      double tot[1];
-      cloth_totals<kPersistThreads>(A, inst, 0, 1, sh, tot);
-      const float alpha = (float)(St.rzh[it & 1] / tot[0]);
-      const int lo = max(s0, A.slice_lo[inst]), hi = min(s1, A.slice_hi[inst]);
+      const float alpha = St.alpha32;
+      const int bjac = St.bjac;
       for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
         const int row = A.slice_row0[sl] + lane;
         float rz = 0.f, rr = 0.f;
@@ -421,7 +508,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
             r[k] = fmaf(-alpha, A.q32[i], A.r32[i]);
             A.r32[i] = r[k];
           }
-          precondition(A, St.bjac, row, r, z);
+          precondition(A, bjac, row, r, z);
 #pragma unroll
           for (int k = 0; k < 3; k++) {
             A.z32[3 * row + k] = z[k];
@@ -436,8 +523,27 @@ __global__ void __launch_bounds__(kPersistThreads) k_mx_persist(Arena A, float e
           A.part32[3 * sl + 2] = rr;
         }
       }
+      if (last_portion(A, inst, hi - lo, &s_flag)) {
+        double tot[2];
+        cloth_totals<kPersistThreads>(A, inst, 1, 2, sh, tot);
+        if (threadIdx.x == 0) {
+          St.inner_iters = it;
+          if (tot[1] <= (double)eta * (double)eta * St.rr_in0 || it >= cap) {
+            St.istop = 1;
+            St.idone = 1;
+            St.red[1] = tot[0];
+            St.red[2] = tot[1];
+            atomicSub(&A.grid_bar[3], 1u);
+          } else {
+            St.beta32 = (float)(tot[0] / St.rzh[it & 1]);
+            St.rzh[(it + 1) & 1] = tot[0];
+          }
+        }
+      }
     }
     if (!grid_sync(A)) return;
+    if (threadIdx.x == 0) s_left = ((volatile unsigned*)A.grid_bar)[3];
+    __syncthreads();
   }
 }
 
@@ -650,6 +756,7 @@ static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm
 void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, int threads,
                                 cudaStream_t s) {
   launch_check(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s), "cudaMemsetAsync");
+  launch_check(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(A.ni, 1), s), "cudaMemsetAsync");
   const int blocks = (A.nslice * 32 + kSliceThreads - 1) / kSliceThreads;
   k_mx_inner_init<<<blocks, kSliceThreads, 0, s>>>(A);
   k_mx_pstart<<<(A.ni * 32 + 127) / 128, 128, 0, s>>>(A);
