@@ -107,18 +107,31 @@ __global__ void k_slot_reduce(Arena A) {
   double acc[9];
 #pragma unroll
   for (int k = 0; k < 9; k++) acc[k] = 0.0;
-  for (int e = A.slot_ptr[s]; e < A.slot_ptr[s + 1]; e++) {
+  // A slot's list holds its triangle blocks, then its stencil blocks (all
+  // triangles are merged before the stencils), so two loops keep warps uniform.
+  const int e_end = A.slot_ptr[s + 1];
+  int e = A.slot_ptr[s];
+  for (; e < e_end; e++) {
     const int code = A.slot_src[e];
-    if (code >= 0) {
-      const double* blk = A.tri_blk + 9 * (size_t)code;
+    if (code < 0) break;
+    const double* blk = A.tri_blk + 9 * (size_t)code;
 #pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] += blk[k];
-    } else {
-      const int c = -code - 1;
-      const int q = c >> 4, a = (c >> 2) & 3, b = c & 3;
-      const double h = A.qK[4 * q + a] * A.qK[4 * q + b] * A.qscale[q];
+    for (int k = 0; k < 9; k++) acc[k] += blk[k];
+  }
+  for (; e < e_end; e++) {
+    const int c = -A.slot_src[e] - 1;
+    const int q = c >> 4, a = (c >> 2) & 3, b = c & 3;
+    const double h = A.qK[4 * q + a] * A.qK[4 * q + b] * A.qscale[q];
+    acc[0] += h;
+    acc[4] += h;
+    acc[8] += h;
+    // the stencil block's off-diagonal entries are +0.0; x + (+0.0) is x
+    // except that -0.0 becomes +0.0, done here on the bits
 #pragma unroll
-      for (int k = 0; k < 9; k++) acc[k] += (k % 4 == 0) ? h : 0.0;
+    for (int k = 0; k < 9; k++) {
+      if (k % 4 == 0) continue;
+      const unsigned long long u = (unsigned long long)__double_as_longlong(acc[k]);
+      if (u == 0x8000000000000000ull) acc[k] = 0.0;
     }
   }
   if (s < A.nb) {
