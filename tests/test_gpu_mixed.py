@@ -103,3 +103,43 @@ def test_mixed_batch_runs(mctx):
         assert st["solver_conv"] < 1e-6
     for i in ids:
         mctx.remove_cloth(i)
+
+
+def _small_sheets(n):
+    rng = np.random.default_rng(11)
+    out = []
+    for i in range(n):
+        side = int(rng.integers(4, 9))
+        r = float(rng.uniform(0.05, 0.2))
+        out.append(scene.square_cloth(side, 0.1 * (side - 1), r + float(rng.uniform(0.02, 0.1)),
+                                      sphere_radius=r, seed=i,
+                                      rotation=float(rng.uniform(0, 6.28)), solver_kind=scene.SOLVER_CG,
+                                      tol=1e-6, maxit=1000))
+    return out
+
+
+def test_mixed_static_cut_same_result_alone():
+    """More than 2048 cloths: the persistent solver keeps a static cut of the
+    slices over its blocks (below that it re-cuts the still-iterating cloths'
+    slices).  Either way each cloth's totals are its own fixed-order sums, so a
+    cloth steps bit-identically in the 2100-cloth arena and alone."""
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    cl = _small_sheets(2100)
+    big = ClothContext(0, "mixed")
+    try:
+        ids = [big.add_cloth(c) for c in cl]
+        big.step(3)
+        many = {i: big.get_state(ids[i]) for i in (0, 777, 2099)}
+        for i in (0, 777, 2099):
+            assert big.stats(ids[i])["solver_conv"] < 1e-6
+    finally:
+        big.close()
+    for i in (0, 777, 2099):
+        one = ClothContext(0, "mixed")
+        try:
+            cid = one.add_cloth(cl[i])
+            one.step(3)
+            x, v = one.get_state(cid)
+        finally:
+            one.close()
+        assert np.array_equal(x, many[i][0]) and np.array_equal(v, many[i][1]), i
