@@ -1,5 +1,5 @@
 // k_mixed.cu -- mixed-precision solve of the implicit system: FP64 iterative
-// refinement around an FP32 block-Jacobi preconditioned CG.
+// refinement around an FP32 CG (block-Jacobi or unpreconditioned, per cloth).
 //
 // The system A dx = b is assembled in FP64 exactly as the reference does; its
 // FP32 copy lives in warp slices (SELL-32: the 32 rows of a slice are a warp's
@@ -7,8 +7,8 @@
 // one coalesced 128-byte line).  Each refinement cycle solves A32 d = r32 to a
 // relative residual eta in FP32 (FP32 arithmetic and accumulation), adds d to
 // dx in FP64 and recomputes r = b - A dx with the FP64 matrix.  Cycles stop at
-// the reference's criterion |r|^2 / |b|^2 < tol^2 (Solve_CG / Solve_PCG,
-// matrix_square_sparse.cpp:338-406, ilu_sparse.cpp:628-709).
+// a decade below the reference's criterion |r|^2 / |b|^2 < tol^2 (Solve_CG /
+// Solve_PCG, matrix_square_sparse.cpp:338-406, ilu_sparse.cpp:628-709).
 #include <algorithm>
 
 #include "kernels.h"
