@@ -315,6 +315,24 @@ def single_cloths(device: int, frames: int = 5, warmup: int = 2) -> dict:
     return out
 
 
+def barrier(world):
+    """All ranks meet here (torch.distributed over gloo when there are several)."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value, world):
+    """The largest value over the ranks: a job's time is its slowest rank's."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def native(args):
     import torch
 
@@ -326,16 +344,15 @@ def native(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        # replicas: each rank steps its own copy of the workload; the side
+        # measurements (plain path, single cloths, serving, CPU sample) are
+        # taken at one GPU only
         import torch.distributed as dist
         dist.init_process_group("gloo")
+        args.no_plain = args.no_single = args.no_serve = args.no_cpu = True
     B.build()
     torch.cuda.set_device(local)
     cloths = scene.config_batch(count=args.cloths)
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
 
     results = {}
     for prec in (["mixed", "fp64"] if args.precision == "both" else [args.precision]):
@@ -345,18 +362,13 @@ def native(args):
         nb_total = sum(int(ctx.pattern(i)[0][-1]) for i in ids)
         stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
         clocks = ClockSampler(local)
-        barrier()
+        barrier(world)
         clocks.start()
         step_ms, prof, counts, launches, start = timed_batch(ctx, ids, args.steps, args.warmup, stream, nv,
                                                              PROFILED)
         clk = clocks.stop()
-        barrier()
-        total_ms = sum(step_ms)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([total_ms], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total_ms = float(t.item())
+        barrier(world)
+        total_ms = max_over_ranks(sum(step_ms), world)
         res = {"value": world * nv * args.steps / (total_ms / 1e3), "ms_per_step": total_ms / args.steps,
                "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
                "prof": prof, "counts": counts, "launches": launches, "clocks": clk, "nv": nv, "nb": nb_total}
@@ -369,6 +381,7 @@ def native(args):
             vs.numpy()[:] = start[1]
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
+            barrier(world)
             e0.record(stream)
             for _ in range(args.steps):
                 ctx.set_states(xs.numpy(), vs.numpy())
@@ -376,7 +389,8 @@ def native(args):
                 ctx.get_states(xs.numpy(), vs.numpy())
             e1.record(stream)
             torch.cuda.synchronize()
-            e2e_ms = e0.elapsed_time(e1)
+            barrier(world)
+            e2e_ms = max_over_ranks(e0.elapsed_time(e1), world)
             res["e2e"] = {"value": world * nv * args.steps / (e2e_ms / 1e3), "unit": UNIT,
                           "h2d_bytes_per_step": 2 * 3 * nv * 8, "d2h_bytes_per_step": 2 * 3 * nv * 8}
             results["headline"] = prec
