@@ -24,7 +24,7 @@ DROPIN_SRC = os.path.join(PKG, "dropin", "clothgpu_dropin.cpp")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
-CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17"]
+CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-pthread"]
 SOURCES = ["topology.cpp", "prof.cu", "k_assemble.cu", "k_solve.cu", "k_mixed.cu", "k_collide.cu", "api.cu",
            "k_noalloc.cu", "serve.cu"]
 
@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None)
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"linking failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -7,8 +7,13 @@
 #include "topology.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <exception>
+#include <memory>
+#include <mutex>
 #include <stdexcept>
+#include <thread>
 #include <utility>
 
 namespace cs {
@@ -88,44 +93,64 @@ class BvhBuilder {
                   (X[v[0] * 3 + 1] + X[v[1] * 3 + 1] + X[v[2] * 3 + 1]) / 3.0,
                   (X[v[0] * 3 + 2] + X[v[1] * 3 + 2] + X[v[2] * 3 + 2]) / 3.0};
     }
-    owner_.assign(nt, 0);
-    node.assign(3, 0);
-    node[0] = -1;
-    node[1] = -1;
-    node[2] = -1;
-    std::vector<int> all(nt);
-    for (int i = 0; i < nt; i++) all[i] = i;
+    owner_.reset(new std::atomic<int>[nt]);
+    for (int i = 0; i < nt; i++) owner_[i].store(0, std::memory_order_relaxed);
+    node.assign(3 * (size_t)(2 * nt - 1), -1);
     if (nt == 1) {
       node[1] = 0;
       return;
     }
-    // depth-first, child 0 subtree completed before child 1 is split, which
-    // reproduces the reference's recursive node numbering
-    std::vector<std::pair<int, std::vector<int>>> work;
-    work.emplace_back(0, std::move(all));
-    while (!work.empty()) {
-      std::pair<int, std::vector<int>> w = std::move(work.back());
-      work.pop_back();
-      std::vector<int> l0, l1;
-      int c0, c1;
-      split(node, w.first, w.second, c0, c1, l0, l1);
-      std::pair<int, std::vector<int>> j0(c0, std::move(l0)), j1(c1, std::move(l1));
-      bool push1 = false, push0 = false;
-      if (j1.second.size() == 1) {
-        node[c1 * 3 + 1] = j1.second[0];
-        node[c1 * 3 + 2] = -1;
-      } else {
-        push1 = true;
+    std::vector<int> all(nt);
+    for (int i = 0; i < nt; i++) all[i] = i;
+    unsigned hc = std::thread::hardware_concurrency();
+    spawn_depth_ = 0;
+    while (spawn_depth_ < 4 && (2u << spawn_depth_) <= hc) spawn_depth_++;
+    subtree(node, 0, std::move(all), 1, 0);
+    if (error_) std::rethrow_exception(error_);
+  }
+
+  // The subtree below node `self`, whose triangles are `list` (more than one).
+  // The reference numbers nodes depth first, child 0's subtree before child 1
+  // is split.  A subtree of m triangles has 2m - 1 nodes, so after a split
+  // into c0 = base and c1 = base + 1, c0's descendants are numbered from
+  // base + 2 and c1's from base + 2 |l0|: subtrees are independent, and the
+  // large ones near the root are built on threads of their own.
+  void subtree(std::vector<int>& node, int self, std::vector<int> list, int base, int depth) {
+    struct Job {
+      int self;
+      std::vector<int> list;
+      int base, depth;
+    };
+    std::vector<std::thread> threads;
+    try {
+      std::vector<Job> work;
+      work.push_back({self, std::move(list), base, depth});
+      while (!work.empty()) {
+        Job w = std::move(work.back());
+        work.pop_back();
+        std::vector<int> l0, l1;
+        const int c0 = w.base, c1 = w.base + 1;
+        split(node, w.self, w.list, c0, c1, l0, l1);
+        const int b0 = w.base + 2, b1 = w.base + 2 * (int)l0.size();
+        if (l1.size() == 1) {
+          node[c1 * 3 + 1] = l1[0];
+        } else if (w.depth < spawn_depth_ && l1.size() >= kParallelMin) {
+          threads.emplace_back([this, &node, c1, b1, d = w.depth + 1, l = std::move(l1)]() mutable {
+            subtree(node, c1, std::move(l), b1, d);
+          });
+        } else {
+          work.push_back({c1, std::move(l1), b1, w.depth + 1});
+        }
+        if (l0.size() == 1)
+          node[c0 * 3 + 1] = l0[0];
+        else
+          work.push_back({c0, std::move(l0), b0, w.depth + 1});
       }
-      if (j0.second.size() == 1) {
-        node[c0 * 3 + 1] = j0.second[0];
-        node[c0 * 3 + 2] = -1;
-      } else {
-        push0 = true;
-      }
-      if (push1) work.push_back(std::move(j1));
-      if (push0) work.push_back(std::move(j0));
+    } catch (...) {
+      std::lock_guard<std::mutex> lk(error_mu_);
+      if (!error_) error_ = std::current_exception();
     }
+    for (std::thread& th : threads) th.join();
   }
 
  private:
@@ -144,8 +169,8 @@ class BvhBuilder {
   }
 
   // DevideTriAryConnex, bvh_aabb.cpp:156-290
-  void split(std::vector<int>& node, int self, const std::vector<int>& list, int& c0, int& c1,
-             std::vector<int>& l0, std::vector<int>& l1) {
+  void split(std::vector<int>& node, int self, const std::vector<int>& list, int c0, int c1, std::vector<int>& l0,
+             std::vector<int>& l1) {
     const double eps = 1.0e-10;
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     bool full = false;
@@ -195,13 +220,14 @@ class BvhBuilder {
       s = seed(list, org, dir);
       if (s == -1) s = list[0];  // every centroid on the plane: not met on sheets
     }
-    c0 = (int)node.size() / 3;
-    c1 = c0 + 1;
-    node.insert(node.end(), {self, -1, -1, self, -1, -1});
+    node[c0 * 3 + 0] = self;
+    node[c1 * 3 + 0] = self;
     node[self * 3 + 1] = c0;
     node[self * 3 + 2] = c1;
-    // flood fill over edge neighbours on the positive side, LIFO
-    owner_[s] = c0;
+    // flood fill over edge neighbours on the positive side, LIFO (a neighbour
+    // in another subtree has an owner other than `self`, whatever its thread
+    // writes there)
+    owner_[s].store(c0, std::memory_order_relaxed);
     l0.push_back(s);
     std::vector<int> stack(1, s);
     while (!stack.empty()) {
@@ -209,24 +235,30 @@ class BvhBuilder {
       stack.pop_back();
       for (int e = 0; e < 3; e++) {
         const int u = across_[t * 3 + e];
-        if (u == -1 || owner_[u] != self) continue;
+        if (u == -1 || owner_[u].load(std::memory_order_relaxed) != self) continue;
         if (dotp(subp(cen_[u], org), dir) < 0) continue;
         stack.push_back(u);
-        owner_[u] = c0;
+        owner_[u].store(c0, std::memory_order_relaxed);
         l0.push_back(u);
       }
     }
     for (int t : list) {
-      if (owner_[t] == c0) continue;
-      owner_[t] = c1;
+      if (owner_[t].load(std::memory_order_relaxed) == c0) continue;
+      owner_[t].store(c1, std::memory_order_relaxed);
       l1.push_back(t);
     }
     if (l1.empty()) throw std::runtime_error("BVH split produced an empty half");
   }
 
+  static constexpr size_t kParallelMin = 8192;  // triangles of a subtree worth a thread
+
   const ClothTopo& t_;
-  std::vector<int> across_, owner_;
+  std::vector<int> across_;
+  std::unique_ptr<std::atomic<int>[]> owner_;  // node that holds each triangle
   std::vector<P3> cen_;
+  int spawn_depth_ = 0;
+  std::mutex error_mu_;
+  std::exception_ptr error_;
 };
 
 }  // namespace
@@ -325,38 +357,53 @@ void build_topology(ClothTopo& t, int np, const double* X0, const int* bc, int n
     const int* p = std::lower_bound(b, e, j);
     return (p != e && *p == j) ? (int)(p - t.col_idx.data()) : -1;
   };
+  // Counted twice over the same element order (count, then fill), so each list
+  // keeps the order in which the reference merges the blocks.
   const int nslot = t.nb + np;
-  std::vector<std::vector<int>> lists(nslot);
-  std::vector<std::vector<int>> glists(np);
+  std::vector<int> tslot(9 * (size_t)nt), qslot(16 * (size_t)nq);
+  t.slot_ptr.assign(nslot + 1, 0);
+  t.grad_ptr.assign(np + 1, 0);
   for (int e = 0; e < nt; e++)
     for (int a = 0; a < 3; a++) {
       const int i = tri[e * 3 + a];
-      glists[i].push_back(e * 3 + a);
+      t.grad_ptr[i + 1]++;
       for (int b = 0; b < 3; b++) {
         const int s = (a == b) ? t.nb + i : slot_of(i, tri[e * 3 + b]);
-        if (s >= 0) lists[s].push_back(e * 9 + a * 3 + b);
+        tslot[e * 9 + a * 3 + b] = s;
+        if (s >= 0) t.slot_ptr[s + 1]++;
       }
     }
   for (int e = 0; e < nq; e++)
     for (int a = 0; a < 4; a++) {
       const int i = quad[e * 4 + a];
-      glists[i].push_back(-(e * 4 + a) - 1);
+      t.grad_ptr[i + 1]++;
       for (int b = 0; b < 4; b++) {
         const int s = (a == b) ? t.nb + i : slot_of(i, quad[e * 4 + b]);
-        if (s >= 0) lists[s].push_back(-(e * 16 + a * 4 + b) - 1);
+        qslot[e * 16 + a * 4 + b] = s;
+        if (s >= 0) t.slot_ptr[s + 1]++;
       }
     }
-  t.slot_ptr.assign(nslot + 1, 0);
-  t.slot_src.clear();
-  for (int s = 0; s < nslot; s++) {
-    t.slot_src.insert(t.slot_src.end(), lists[s].begin(), lists[s].end());
-    t.slot_ptr[s + 1] = (int)t.slot_src.size();
-  }
-  t.grad_ptr.assign(np + 1, 0);
-  t.grad_src.clear();
-  for (int v = 0; v < np; v++) {
-    t.grad_src.insert(t.grad_src.end(), glists[v].begin(), glists[v].end());
-    t.grad_ptr[v + 1] = (int)t.grad_src.size();
+  for (int s = 0; s < nslot; s++) t.slot_ptr[s + 1] += t.slot_ptr[s];
+  for (int v = 0; v < np; v++) t.grad_ptr[v + 1] += t.grad_ptr[v];
+  t.slot_src.resize(t.slot_ptr[nslot]);
+  t.grad_src.resize(t.grad_ptr[np]);
+  {
+    std::vector<int> fill(t.slot_ptr.begin(), t.slot_ptr.end() - 1);
+    std::vector<int> gfill(t.grad_ptr.begin(), t.grad_ptr.end() - 1);
+    for (int e = 0; e < nt; e++) {
+      for (int a = 0; a < 3; a++) t.grad_src[gfill[tri[e * 3 + a]]++] = e * 3 + a;
+      for (int k = 0; k < 9; k++) {
+        const int s = tslot[e * 9 + k];
+        if (s >= 0) t.slot_src[fill[s]++] = e * 9 + k;
+      }
+    }
+    for (int e = 0; e < nq; e++) {
+      for (int a = 0; a < 4; a++) t.grad_src[gfill[quad[e * 4 + a]]++] = -(e * 4 + a) - 1;
+      for (int k = 0; k < 16; k++) {
+        const int s = qslot[e * 16 + k];
+        if (s >= 0) t.slot_src[fill[s]++] = -(e * 16 + k) - 1;
+      }
+    }
   }
 
   // block ILU(0) schedule (DoILUDecomp, ilu_sparse.cpp:507-569): row i waits for
