@@ -159,6 +159,8 @@ class ClothContext:
         return out
 
     def pattern(self, cid):
+        """Block pattern of the cloth's matrix (CMatrixSquareSparse::SetPattern,
+        matrix_square_sparse.cpp:140-165): row pointer and sorted columns."""
         nb = ctypes.c_int()
         self._ck(self.L.cs_pattern(self.h, cid, ctypes.byref(nb), None, None))
         rp = np.zeros(self.np[cid] + 1, np.int32)
@@ -167,6 +169,9 @@ class ClothContext:
         return rp, ci
 
     def assemble(self, cid, x, v):
+        """Implicit system at (x, v): AddWdWddW_Cloth / _Contact / Mearge /
+        SetBoundaryCondition (solve_internal_sparse.h:19-183, matrix_square_sparse.cpp:88-302).
+        Returns the diagonal and off-diagonal blocks and the right-hand side."""
         nb = ctypes.c_int()
         self._ck(self.L.cs_pattern(self.h, cid, ctypes.byref(nb), None, None))
         n = self.np[cid]
@@ -178,6 +183,8 @@ class ClothContext:
         return vd, vc, b
 
     def ilu(self, cid):
+        """Block ILU(0) of the last assembled matrix: SetValueILU and DoILUDecomp
+        (ilu_sparse.cpp:352-624).  Returns the factor blocks and the singular-pivot count."""
         nb = ctypes.c_int()
         self._ck(self.L.cs_pattern(self.h, cid, ctypes.byref(nb), None, None))
         fd = np.zeros(9 * self.np[cid])
@@ -187,6 +194,7 @@ class ClothContext:
         return fd, fc, ns.value
 
     def pcg(self, cid, b, tol, maxit):
+        """Solve_PCG with the ILU(0) factor (ilu_sparse.cpp:628-709)."""
         x = np.zeros(3 * self.np[cid])
         conv = ctypes.c_double()
         it = ctypes.c_int()
@@ -195,6 +203,7 @@ class ClothContext:
         return x, conv.value, it.value
 
     def cg(self, cid, b, tol, maxit):
+        """Solve_CG, unpreconditioned (matrix_square_sparse.cpp:338-406)."""
         x = np.zeros(3 * self.np[cid])
         conv = ctypes.c_double()
         it = ctypes.c_int()
@@ -203,11 +212,15 @@ class ClothContext:
         return x, conv.value, it.value
 
     def spmv(self, cid, x):
+        """y = A x with the last assembled matrix (CMatrixSquareSparse::MatVec,
+        matrix_square_sparse.cpp:167-270)."""
         y = np.zeros(3 * self.np[cid])
         self._ck(self.L.cs_spmv(self.h, cid, N.dp(np.ascontiguousarray(x, np.float64)), N.dp(y)))
         return y
 
     def bvh_nodes(self, cid):
+        """BVH nodes (parent, child 0, child 1; child 1 = -1 at a leaf) as
+        MakeBVHTopology_TopDown builds them (bvh_aabb.cpp:109-313)."""
         nn = ctypes.c_int()
         self._ck(self.L.cs_bvh_nodes(self.h, cid, ctypes.byref(nn), None))
         out = np.zeros(3 * nn.value, np.int32)
@@ -220,11 +233,13 @@ class ClothContext:
         return nn.value
 
     def refit_prx(self, cid, x, delta):
+        """Node boxes for proximity (BuildBoundingBoxChild_Prx, bvh_aabb.cpp:23-61)."""
         out = np.zeros(7 * self._nnode(cid))
         self._ck(self.L.cs_refit_prx(self.h, cid, N.dp(np.ascontiguousarray(x, np.float64)), delta, N.dp(out)))
         return out.reshape(-1, 7)
 
     def refit_ccd(self, cid, x, v, dt):
+        """Swept node boxes (BuildBoundingBoxChild_CCD, bvh_aabb.cpp:64-106)."""
         out = np.zeros(7 * self._nnode(cid))
         self._ck(self.L.cs_refit_ccd(self.h, cid, N.dp(np.ascontiguousarray(x, np.float64)),
                                      N.dp(np.ascontiguousarray(v, np.float64)), dt, N.dp(out)))
@@ -242,15 +257,19 @@ class ClothContext:
             return out[: 5 * n.value].reshape(-1, 5)
 
     def contacts_prx(self, cid, x, delta):
+        """Proximity contact set in std::set order (GetContactElement_Proximity,
+        bvh_aabb.cpp:441-557): rows (i0, i1, i2, i3, is_fv)."""
         xa = np.ascontiguousarray(x, np.float64)
         return self._contacts(self.L.cs_contacts_prx, self.h, cid, N.dp(xa), delta)
 
     def contacts_ccd(self, cid, x, v, dt, delta):
+        """CCD contact set in std::set order (GetContactElement_CCD, bvh_aabb.cpp:797-923)."""
         xa = np.ascontiguousarray(x, np.float64)
         va = np.ascontiguousarray(v, np.float64)
         return self._contacts(self.L.cs_contacts_ccd, self.h, cid, N.dp(xa), N.dp(va), dt, delta)
 
     def impulse_prx(self, cid, x, v, ce):
+        """SelfCollisionImpulse_Proximity over the contacts ce (self_collision_cloth.cpp:20-112)."""
         v = np.array(v, np.float64)
         ce = np.ascontiguousarray(ce, np.int32)
         self._ck(self.L.cs_impulse_prx(self.h, cid, N.dp(np.ascontiguousarray(x, np.float64)), N.dp(v), N.ip(ce),
@@ -258,6 +277,7 @@ class ClothContext:
         return v
 
     def impulse_ccd(self, cid, x, v, ce):
+        """SelfCollisionImpulse_CCD over the contacts ce (self_collision_cloth.cpp:116-212)."""
         v = np.array(v, np.float64)
         ce = np.ascontiguousarray(ce, np.int32)
         self._ck(self.L.cs_impulse_ccd(self.h, cid, N.dp(np.ascontiguousarray(x, np.float64)), N.dp(v), N.ip(ce),
@@ -265,19 +285,23 @@ class ClothContext:
         return v
 
     def riz_reset(self, cid):
+        """Empties the cloth's rigid impact zones."""
         self._ck(self.L.cs_riz_reset(self.h, cid))
 
     def riz_add(self, cid, ce):
+        """MakeRigidImpactZone with the contacts ce (self_collision_cloth.cpp:220-274)."""
         ce = np.ascontiguousarray(ce, np.int32)
         self._ck(self.L.cs_riz_add(self.h, cid, N.ip(ce), ce.shape[0]))
 
     def riz_zones(self, cid):
+        """Zone of every vertex (-1 outside all zones) and the number of zones."""
         z = np.zeros(self.np[cid], np.int32)
         nz = ctypes.c_int()
         self._ck(self.L.cs_riz_zones(self.h, cid, N.ip(z), ctypes.byref(nz)))
         return z, nz.value
 
     def riz_apply(self, cid, x, v, v0):
+        """ApplyRigidImpactZone (self_collision_cloth.cpp:298-348)."""
         v = np.array(v, np.float64)
         self._ck(self.L.cs_riz_apply(self.h, cid, N.dp(np.ascontiguousarray(x, np.float64)), N.dp(v),
                                      N.dp(np.ascontiguousarray(v0, np.float64))))
@@ -285,6 +309,7 @@ class ClothContext:
 
     # ---- element batches ---------------------------------------------------------------
     def element_cst(self, C, c, lam, myu):
+        """WdWddW_CST per triangle (cloth_internal_physics.h:70-176)."""
         C = np.ascontiguousarray(C, np.float64).reshape(-1, 9)
         c = np.ascontiguousarray(c, np.float64).reshape(-1, 9)
         n = C.shape[0]
@@ -293,6 +318,7 @@ class ClothContext:
         return W, dW, ddW
 
     def element_bend(self, C, c, stiff):
+        """WdWddW_Bend per stencil (cloth_internal_physics.h:180-238)."""
         C = np.ascontiguousarray(C, np.float64).reshape(-1, 12)
         c = np.ascontiguousarray(c, np.float64).reshape(-1, 12)
         n = C.shape[0]
@@ -301,6 +327,7 @@ class ClothContext:
         return W, dW, ddW
 
     def element_contact(self, c, params):
+        """WdWddW_Contact per vertex with the cloth's obstacle (cloth_internal_physics.h:243-280)."""
         c = np.ascontiguousarray(c, np.float64).reshape(-1, 3)
         n = c.shape[0]
         W, dW, ddW = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 9))
