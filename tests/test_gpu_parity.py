@@ -74,12 +74,18 @@ def test_elements_bit_exact(ctx, oracle_port):
     for k in range(0, 500, 7):
         w, dw, ddw = O.wdwddw_cst(oracle_port, C[k], c[k], 1.0, 1.0)
         assert W[k] == w and np.array_equal(dW[k], dw) and np.array_equal(ddW[k], ddw)
-    prm = scene.Params(obs_radius=0.3)
-    p = rng.uniform(-0.35, 0.35, (300, 3))
-    W, dW, ddW = ctx.element_contact(p, prm)
-    for k in range(300):
-        w, dw, ddw = O.wdwddw_contact(oracle_port, p[k], prm)
-        assert W[k] == w and np.array_equal(dW[k], dw) and np.array_equal(ddW[k], ddw)
+    # every obstacle descriptor: none, the demo's plane, the solid sphere, the
+    # demo's inside-out sphere (points on both sides of each surface)
+    for kind, center, radius in [(scene.OBSTACLE_NONE, (0.0, 0.0, 0.0), 0.3),
+                                 (scene.OBSTACLE_PLANE_Z, (0.0, 0.0, -0.05), 0.0),
+                                 (scene.OBSTACLE_SPHERE_SOLID, (0.0, 0.0, 0.0), 0.3),
+                                 (scene.OBSTACLE_SPHERE_HOLLOW, (0.05, 0.0, 0.1), 0.3)]:
+        prm = scene.Params(obs_radius=radius, obstacle_kind=kind, obs_center=center)
+        p = rng.uniform(-0.35, 0.35, (300, 3))
+        W, dW, ddW = ctx.element_contact(p, prm)
+        for k in range(300):
+            w, dw, ddw = O.wdwddw_contact(oracle_port, p[k], prm)
+            assert W[k] == w and np.array_equal(dW[k], dw) and np.array_equal(ddW[k], ddw), (kind, k)
 
 
 @pytest.mark.parametrize("name", ["small_21", "fold_31"])
