@@ -435,6 +435,10 @@ struct co_cloth {
   int *zone_of;
   /* scratch */
   double *tmp0, *tmp1, *tmp2, *tmp3;
+  /* contact log of the last co_resolve: one entry per detection */
+  int log_on, log_n, log_cap;
+  int *log_kind, *log_count;
+  unsigned long long *log_digest;
 };
 
 static void *xmalloc(size_t n) {
@@ -597,6 +601,9 @@ void co_destroy(co_cloth *h) {
   free(h->tmp1);
   free(h->tmp2);
   free(h->tmp3);
+  free(h->log_kind);
+  free(h->log_count);
+  free(h->log_digest);
   free(h);
 }
 
@@ -978,6 +985,33 @@ void co_pcg(co_cloth *h, const double *b, double tol, int maxit, double *x, doub
 void co_cg(co_cloth *h, const double *b, double tol, int maxit, double *x, double *conv, int *iter) {
   memcpy(h->tmp0, b, sizeof(double) * 3 * (size_t)h->np);
   cg_solve(h, h->tmp0, x, tol, maxit, conv, iter);
+}
+
+/* the residual r_vec that the last co_cg / co_pcg left behind */
+void co_last_residual(const co_cloth *h, double *r) { memcpy(r, h->tmp0, sizeof(double) * 3 * (size_t)h->np); }
+
+/* CPreconditionerILU::Solve (ilu_sparse.h:23-26) with the last co_ilu factor */
+void co_ilu_solve(const co_cloth *h, double *vec) { ilu_apply(h, vec); }
+
+/* MatVec(alpha, x, beta, y) on the last assembled matrix, 3x3 branch of
+ * matrix_square_sparse.cpp:218-242 */
+void co_matvec(const co_cloth *h, double alpha, const double *x, double beta, double *y) {
+  int i, s, r;
+  for (i = 0; i < h->np; i++) {
+    double *yi = y + i * 3;
+    for (r = 0; r < 3; r++) yi[r] *= beta;
+    for (s = h->row_ptr[i]; s < h->row_ptr[i + 1]; s++) {
+      const int j = h->col_idx[s];
+      const double *a = h->vcrs + (size_t)s * 9;
+      for (r = 0; r < 3; r++)
+        yi[r] += alpha * (a[r * 3 + 0] * x[j * 3 + 0] + a[r * 3 + 1] * x[j * 3 + 1] + a[r * 3 + 2] * x[j * 3 + 2]);
+    }
+    {
+      const double *a = h->vdia + (size_t)i * 9;
+      for (r = 0; r < 3; r++)
+        yi[r] += alpha * (a[r * 3 + 0] * x[i * 3 + 0] + a[r * 3 + 1] * x[i * 3 + 1] + a[r * 3 + 2] * x[i * 3 + 2]);
+    }
+  }
 }
 
 /* One Newton step of backward Euler, StepTime_InternalDynamicsILU
@@ -1651,6 +1685,18 @@ static int collect(co_cloth *h, const double *x, const double *v, double dt, dou
   return n;
 }
 
+/* DistanceFaceVertex / DistanceEdgeEdge / FindCoplanerInterp
+ * (bvh_aabb.cpp:321-384, 598-662) on 12 doubles of points */
+double co_distance_fv(const double *p, double *w) {
+  return dist_face_vertex(at(p, 0), at(p, 1), at(p, 2), at(p, 3), w, w + 1);
+}
+double co_distance_ee(const double *p, double *r) {
+  return dist_edge_edge(at(p, 0), at(p, 1), at(p, 2), at(p, 3), r, r + 1);
+}
+double co_coplanar_time(const double *s, const double *e) {
+  return coplanar_time(at(s, 0), at(s, 1), at(s, 2), at(s, 3), at(e, 0), at(e, 1), at(e, 2), at(e, 3));
+}
+
 int co_contacts_prx(co_cloth *h, const double *x, double delta, int *out, int cap) {
   co_refit_prx(h, x, delta, NULL);
   return collect(h, x, NULL, 0, delta, 0, out, cap);
@@ -1926,6 +1972,47 @@ static int *grow_ce(int *buf, int *cap, int need) {
   return buf;
 }
 
+/* FNV-1a over the 32-bit words of an ordered contact list (5 words a contact) */
+unsigned long long co_contact_digest(const int *ce, int n) {
+  unsigned long long d = 14695981039346656037ULL;
+  long long i;
+  for (i = 0; i < 5LL * n; i++) {
+    d ^= (unsigned long long)(unsigned int)ce[i];
+    d *= 1099511628211ULL;
+  }
+  return d;
+}
+
+static void log_detection(co_cloth *h, int ccd, const int *ce, int n) {
+  if (!h->log_on) return;
+  if (h->log_n == h->log_cap) {
+    h->log_cap = h->log_cap ? 2 * h->log_cap : 16;
+    h->log_kind = (int *)realloc(h->log_kind, sizeof(int) * (size_t)h->log_cap);
+    h->log_count = (int *)realloc(h->log_count, sizeof(int) * (size_t)h->log_cap);
+    h->log_digest = (unsigned long long *)realloc(h->log_digest, sizeof(unsigned long long) * (size_t)h->log_cap);
+    if (!h->log_kind || !h->log_count || !h->log_digest) abort();
+  }
+  h->log_kind[h->log_n] = ccd;
+  h->log_count[h->log_n] = n;
+  h->log_digest[h->log_n] = co_contact_digest(ce, n);
+  h->log_n++;
+}
+
+void co_contact_log(co_cloth *h, int enable) {
+  h->log_on = enable != 0;
+  h->log_n = 0;
+}
+
+int co_contact_log_read(const co_cloth *h, int *kind, int *count, unsigned long long *digest, int cap) {
+  int i;
+  for (i = 0; i < h->log_n && i < cap; i++) {
+    kind[i] = h->log_kind[i];
+    count[i] = h->log_count[i];
+    digest[i] = h->log_digest[i];
+  }
+  return h->log_n;
+}
+
 static int contacts_alloc(co_cloth *h, const double *x, const double *v, int ccd, int **buf, int *cap) {
   const co_params *q = &h->prm;
   int n;
@@ -1940,6 +2027,7 @@ static int contacts_alloc(co_cloth *h, const double *x, const double *v, int ccd
     *buf = grow_ce(*buf, cap, n);
     n = collect(h, x, v, q->dt, q->contact_clearance, ccd, *buf, *cap);
   }
+  log_detection(h, ccd, *buf, n);
   return n;
 }
 
@@ -1950,6 +2038,7 @@ void co_resolve(co_cloth *h, const double *x1, double *v, co_stats *st) {
   int *ce = NULL;
   co_stats s;
   memset(&s, 0, sizeof(s));
+  h->log_n = 0;
   if (st) {
     s.solver_iterations = st->solver_iterations;
     s.solver_conv = st->solver_conv;

@@ -103,6 +103,13 @@ void co_pcg(co_cloth *h, const double *b, double tol, int maxit, double *x,
 void co_cg(co_cloth *h, const double *b, double tol, int maxit, double *x,
            double *conv, int *iter);                  /* after co_assemble */
 void co_implicit(co_cloth *h, double *x, double *v, co_stats *st);
+void co_last_residual(const co_cloth *h, double *r);   /* r_vec after co_cg / co_pcg */
+void co_ilu_solve(const co_cloth *h, double *vec);     /* after co_ilu */
+void co_matvec(const co_cloth *h, double alpha, const double *x, double beta, double *y); /* after co_assemble */
+/* geometry on 12 doubles of points (face p0 p1 p2 + vertex p3; edges p0 p1, q0 q1) */
+double co_distance_fv(const double *p, double *w);
+double co_distance_ee(const double *p, double *r);
+double co_coplanar_time(const double *s, const double *e);
 
 /* collision pieces */
 void co_refit_prx(co_cloth *h, const double *x, double delta, double *boxes);
@@ -120,6 +127,14 @@ void co_resolve(co_cloth *h, const double *x1, double *v, co_stats *st);
 void co_update_velocity(co_cloth *h, const double *x, double *v);
 /* MakeNormal (self_contact_sparse/main.cpp:183-211): unit vertex normals */
 void co_vertex_normals(const co_cloth *h, const double *x, double *nrm);
+
+/* Contact log: with logging on, co_resolve (and so co_step) records one entry
+ * per detection it runs, in order: kind (0 proximity, 1 swept/CCD), contact
+ * count and co_contact_digest of the ordered list (5 ints a contact: is_fv,
+ * then the canonical key).  co_contact_log clears the log. */
+unsigned long long co_contact_digest(const int *ce, int n);
+void co_contact_log(co_cloth *h, int enable);
+int co_contact_log_read(const co_cloth *h, int *kind, int *count, unsigned long long *digest, int cap);
 
 /* one frame of self_contact_sparse/main.cpp StepTime, in place on x, v */
 void co_step(co_cloth *h, double *x, double *v, co_stats *st);

@@ -21,7 +21,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libclothoracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libclothref.so")
-REF_SRC = os.environ.get("CLOTH_REFERENCE_DIR", "/root/reference")
+# the reference checkout: CLOTH_REFERENCE_DIR, else beside this repository's checkout
+REF_SRC = os.environ.get("CLOTH_REFERENCE_DIR", os.path.normpath(os.path.join(HERE, "..", "..", "reference")))
 
 
 class CoParams(ctypes.Structure):
@@ -141,6 +142,19 @@ class OracleLib:
         self.update_velocity = f("update_velocity", None, _V, _D, _D)
         self.vertex_normals = f("vertex_normals", None, _V, _D, _D)
         self.step = f("step", None, _V, _D, _D, S)
+        self.last_residual = f("last_residual", None, _V, _D)
+        self.ilu_solve = f("ilu_solve", None, _V, _D)
+        self.matvec = f("matvec", None, _V, ctypes.c_double, _D, ctypes.c_double, _D)
+        self.distance_fv = f("distance_fv", ctypes.c_double, _D, _D)
+        self.distance_ee = f("distance_ee", ctypes.c_double, _D, _D)
+        self.coplanar_time = f("coplanar_time", ctypes.c_double, _D, _D)
+        # contact log (restatement only: the reference keeps no per-pass record)
+        self.has_log = hasattr(L, pre + "contact_log")
+        if self.has_log:
+            self.contact_log = f("contact_log", None, _V, ctypes.c_int)
+            self.contact_log_read = f("contact_log_read", ctypes.c_int, _V, _I, _I,
+                                      ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int)
+            self.contact_digest = f("contact_digest", ctypes.c_ulonglong, _I, ctypes.c_int)
 
 
 class OracleCloth:
@@ -229,6 +243,24 @@ class OracleCloth:
                   ctypes.byref(it))
         return x, conv.value, it.value
 
+    def last_residual(self):
+        """r_vec left by the last cg / pcg."""
+        r = np.zeros(3 * self.n)
+        self.L.last_residual(self.h, _dp(r))
+        return r
+
+    def ilu_solve(self, vec):
+        """CPreconditionerILU::Solve with the last ilu() factor."""
+        z = np.array(vec, dtype=np.float64)
+        self.L.ilu_solve(self.h, _dp(z))
+        return z
+
+    def matvec(self, alpha, x, beta, y):
+        """MatVec(alpha, x, beta, y) on the last assembled matrix."""
+        y = np.array(y, dtype=np.float64)
+        self.L.matvec(self.h, alpha, _dp(np.ascontiguousarray(x, dtype=np.float64)), beta, _dp(y))
+        return y
+
     def implicit(self, x, v):
         x = np.array(x, dtype=np.float64)
         v = np.array(v, dtype=np.float64)
@@ -306,6 +338,24 @@ class OracleCloth:
         self.L.vertex_normals(self.h, _dp(np.ascontiguousarray(x, dtype=np.float64)), _dp(out))
         return out
 
+    def log_contacts(self, enable: bool = True):
+        """Record, per detection of the following resolve / step, (kind,
+        count, digest of the ordered contact list)."""
+        self.L.contact_log(self.h, int(enable))
+
+    def contact_log(self):
+        """The detections of the last resolve: a list of (ccd, count, digest)."""
+        cap = 256
+        while True:
+            k = np.zeros(cap, np.int32)
+            c = np.zeros(cap, np.int32)
+            d = np.zeros(cap, np.uint64)
+            n = self.L.contact_log_read(self.h, _ip(k), _ip(c),
+                                        d.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), cap)
+            if n <= cap:
+                return [(int(k[i]), int(c[i]), int(d[i])) for i in range(n)]
+            cap = n
+
     def step(self, nsteps: int = 1):
         stats = []
         for _ in range(nsteps):
@@ -341,3 +391,23 @@ def wdwddw_contact(lib: OracleLib, c, params):
     lib.wdwddw_contact(_dp(np.ascontiguousarray(c, np.float64)), ctypes.byref(prm), ctypes.byref(W),
                        _dp(dW), _dp(ddW))
     return W.value, dW, ddW
+
+
+def distance_fv(lib: OracleLib, pts):
+    """DistanceFaceVertex on 12 doubles (face p0 p1 p2, vertex p3): (dist, w0, w1)."""
+    w = np.zeros(2)
+    d = lib.distance_fv(_dp(np.ascontiguousarray(pts, dtype=np.float64)), _dp(w))
+    return d, w[0], w[1]
+
+
+def distance_ee(lib: OracleLib, pts):
+    """DistanceEdgeEdge on 12 doubles (p0 p1 q0 q1): (dist, ratio_p, ratio_q)."""
+    r = np.zeros(2)
+    d = lib.distance_ee(_dp(np.ascontiguousarray(pts, dtype=np.float64)), _dp(r))
+    return d, r[0], r[1]
+
+
+def coplanar_time(lib: OracleLib, s, e):
+    """FindCoplanerInterp on start / end points (12 doubles each)."""
+    return lib.coplanar_time(_dp(np.ascontiguousarray(s, dtype=np.float64)),
+                             _dp(np.ascontiguousarray(e, dtype=np.float64)))

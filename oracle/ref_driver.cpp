@@ -106,6 +106,7 @@ struct RefCloth {
   CJaggedArray aEdge;
   std::vector<std::set<int> > aRIZ;
   std::vector<double> vec_b;  // rhs of the last assembly
+  std::vector<double> r_last; // r_vec of the last Solve_CG / Solve_PCG
 };
 
 std::vector<CContactElement> to_elems(const int* ce, int n) {
@@ -320,6 +321,7 @@ void ref_pcg(void* p, const double* b, double tol, int maxit, double* x, double*
   memcpy(x, u.data(), sizeof(double) * nDof);
   *conv = c;
   *iter = it;
+  h->r_last = r;
 }
 
 void ref_cg(void* p, const double* b, double tol, int maxit, double* x, double* conv, int* iter) {
@@ -332,6 +334,41 @@ void ref_cg(void* p, const double* b, double tol, int maxit, double* x, double* 
   memcpy(x, u.data(), sizeof(double) * nDof);
   *conv = c;
   *iter = it;
+  h->r_last = r;
+}
+
+void ref_last_residual(void* p, double* r) {
+  RefCloth* h = (RefCloth*)p;
+  memcpy(r, h->r_last.data(), sizeof(double) * h->r_last.size());
+}
+
+void ref_ilu_solve(void* p, double* vec) {
+  RefCloth* h = (RefCloth*)p;
+  std::vector<double> v(vec, vec + 3 * h->mat_A.m_nblk);
+  h->ilu_A->Solve(v);
+  memcpy(vec, v.data(), sizeof(double) * v.size());
+}
+
+void ref_matvec(void* p, double alpha, const double* x, double beta, double* y) {
+  RefCloth* h = (RefCloth*)p;
+  const int nDof = 3 * h->mat_A.m_nblk;
+  std::vector<double> xv(x, x + nDof), yv(y, y + nDof);
+  h->mat_A.MatVec(alpha, xv, beta, yv);
+  memcpy(y, yv.data(), sizeof(double) * nDof);
+}
+
+static CVector3D v3(const double* a, int k) { return CVector3D(a[3 * k], a[3 * k + 1], a[3 * k + 2]); }
+
+double ref_distance_fv(const double* pt, double* w) {
+  return DistanceFaceVertex(v3(pt, 0), v3(pt, 1), v3(pt, 2), v3(pt, 3), w[0], w[1]);
+}
+
+double ref_distance_ee(const double* pt, double* r) {
+  return DistanceEdgeEdge(v3(pt, 0), v3(pt, 1), v3(pt, 2), v3(pt, 3), r[0], r[1]);
+}
+
+double ref_coplanar_time(const double* s, const double* e) {
+  return FindCoplanerInterp(v3(s, 0), v3(s, 1), v3(s, 2), v3(s, 3), v3(e, 0), v3(e, 1), v3(e, 2), v3(e, 3));
 }
 
 // StepTime_InternalDynamicsILU / StepTime_InternalDynamics with the solver tolerance

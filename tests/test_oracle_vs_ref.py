@@ -97,3 +97,49 @@ def test_obstacles_and_materials(oracle_port, oracle_ref, obstacle, center, radi
     else:
         touched = True
     assert touched
+
+
+def test_matrix_functions_match_reference(oracle_port, oracle_ref):
+    """MatVec with general alpha / beta, Solve_CG and Solve_PCG with the residual
+    they leave in r_vec, DoILUDecomp and CPreconditionerILU::Solve: the
+    restatement equals the reference bit for bit on an assembled system,
+    including a CG cut off by its iteration cap."""
+    c = scene.config_small()
+    a = O.OracleCloth(oracle_port, c)
+    b = O.OracleCloth(oracle_ref, c)
+    a.step(30)
+    x, v = a.x.copy(), a.v.copy()
+    va, vb = a.assemble(x, v), b.assemble(x, v)
+    for p, q in zip(va, vb):
+        assert np.array_equal(p, q)
+    rhs = va[2]
+    rng = np.random.default_rng(7)
+    xs, ys = rng.normal(size=rhs.size), rng.normal(size=rhs.size)
+    for alpha, beta in ((1.0, 0.0), (0.5, 2.0), (-1.25, 0.75)):
+        assert np.array_equal(a.matvec(alpha, xs, beta, ys), b.matvec(alpha, xs, beta, ys))
+    for tol, maxit in ((1e-6, 1000), (1e-6, 5)):
+        ra, rb = a.cg(rhs, tol, maxit), b.cg(rhs, tol, maxit)
+        assert np.array_equal(ra[0], rb[0]) and ra[1:] == rb[1:]
+        assert np.array_equal(a.last_residual(), b.last_residual())
+    fa, fb = a.ilu(), b.ilu()
+    assert np.array_equal(fa[0], fb[0]) and np.array_equal(fa[1], fb[1]) and fa[2] == fb[2]
+    assert np.array_equal(a.ilu_solve(rhs), b.ilu_solve(rhs))
+    pa, pb = a.pcg(rhs, 1e-6, 100), b.pcg(rhs, 1e-6, 100)
+    assert np.array_equal(pa[0], pb[0]) and pa[1:] == pb[1:]
+    assert np.array_equal(a.last_residual(), b.last_residual())
+
+
+def test_geometry_functions_match_reference(oracle_port, oracle_ref):
+    """DistanceFaceVertex, DistanceEdgeEdge (both branches) and
+    FindCoplanerInterp (roots, no roots, the quadratic case) bit for bit."""
+    rng = np.random.default_rng(99)
+    for k in range(300):
+        p = rng.uniform(-1, 1, 12)
+        if k % 5 == 0:  # parallel edges
+            p[9:12] = p[6:9] + 0.5 * (p[3:6] - p[0:3])
+        assert O.distance_fv(oracle_port, p) == O.distance_fv(oracle_ref, p)
+        assert O.distance_ee(oracle_port, p) == O.distance_ee(oracle_ref, p)
+        e = p + rng.normal(0, 0.3 if k % 3 else 1e-3, 12)
+        if k % 7 == 0:  # equal displacement of all points: the cubic degenerates
+            e = p + np.tile(rng.normal(0, 0.2, 3), 4)
+        assert O.coplanar_time(oracle_port, p, e) == O.coplanar_time(oracle_ref, p, e)
