@@ -34,15 +34,18 @@ METRIC = "vertex-steps/s batched vs plain GPU path at 1e-6 err; p50/p99 step lat
 UNIT = "vertex-steps/s"
 
 
-def workload_config(n_cloths: int, nv: int, precision: str) -> dict:
+def workload_config(n_cloths: int, nv: int) -> dict:
     return {
         "workload": f"{n_cloths} cloths in one arena, grid side U{{11..81}} (1 m), drop 0.3-1.5 m onto "
                     f"spheres r 0.1-0.4 m, CG tol 1e-6, dt 0.02",
         "cloths": n_cloths,
         "vertices": nv,
-        "precision": precision,
         "l2": "inputs larger than L2 (FP64 block matrix of the arena > 1 GB)",
     }
+
+
+def workload_vertices(cloths) -> int:
+    return int(sum(c.np for c in cloths))
 
 
 def read_peaks() -> dict:
@@ -52,6 +55,29 @@ def read_peaks() -> dict:
         return {"hbm_gbs": float(p["hbm_gbs"]), "source": "measured"}
     except Exception:
         return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_figures() -> dict:
+    """Figures from the committed ncu summaries that the bench cannot measure
+    itself: lines of the form `bench-figure <kernel> <name> <value>` in
+    profiles/*.md, e.g. the ratio of DRAM bytes to algorithmic bytes of a kernel
+    (scaled here to a launch of this run) or its FP64-pipe activity."""
+    out = {}
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return out
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith(".md"):
+            continue
+        with open(os.path.join(d, fn)) as f:
+            for line in f:
+                p = line.strip().strip("`").split()
+                if len(p) == 4 and p[0] == "bench-figure":
+                    try:
+                        out[(p[1], p[2])] = float(p[3])
+                    except ValueError:
+                        pass
+    return out
 
 
 class ClockSampler:
@@ -138,20 +164,21 @@ def run_cpu_baseline(cloths, budget_s: float = 12.0) -> dict:
 
 
 # --------------------------------------------------------------------------------------
-def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
-    """K resident frames of every cloth in the context; per-frame CUDA events on
-    the library's stream.  Returns (per-frame ms list, profile dict, launches)."""
+def timed_batch(ctx, steps, warmup, stream, nv):
+    """W untimed frames, then K frames of every cloth in the context timed with
+    per-frame CUDA events on the library's stream (no per-kernel profiling).
+    Returns (per-frame ms list, launches, start state of the timed frames)."""
     import torch
 
     ctx.step(warmup)
     ctx.synchronize()
     torch.cuda.synchronize()
-    # the state at the start of the timed frames (the end-to-end run replays them)
+    # the state at the start of the timed frames (the end-to-end and profiled
+    # passes replay the same frames from it)
     x0 = np.empty(3 * nv)
     v0 = np.empty(3 * nv)
     ctx.get_states(x0, v0)
     launches0 = ctx.launch_count()
-    ctx.profile(True)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
     ev[0].record(stream)
     for k in range(steps):
@@ -160,6 +187,17 @@ def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
     torch.cuda.synchronize()
     ctx.synchronize()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    return step_ms, ctx.launch_count() - launches0, (x0, v0)
+
+
+def profiled_replay(ctx, steps, start, profile_names=()):
+    """The timed frames once more from their start state, with CUDA events around
+    every kernel launch: per-class kernel time and launches, and the device
+    counters (contacts, FP64 tests, algorithmic bytes of the solver)."""
+    ctx.set_states(start[0], start[1])
+    ctx.profile(True)
+    ctx.step(steps)
+    ctx.synchronize()
     prof = {name: ctx.profile_read(name) for name in profile_names}
     counts = {}
     counts["spmv32_bytes"], counts["spmv64_bytes"] = ctx.profile_bytes()
@@ -167,7 +205,7 @@ def timed_batch(ctx, ids, steps, warmup, stream, nv, profile_names=()):
               "fp64_ee_ccd", "persist_bytes"):
         counts[k] = ctx.profile_read(k)[1]
     ctx.profile(False)
-    return step_ms, prof, counts, ctx.launch_count() - launches0, (x0, v0)
+    return prof, counts
 
 
 PROFILED = ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit", "traverse",
@@ -175,33 +213,75 @@ PROFILED = ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce
             "mx_persist")
 
 
-def plain_one_per_launch(cloths, device, frames: int, budget_s: float = 8.0) -> dict:
-    """The plain FP64 path, one cloth per arena and launch sequence, on a sample."""
+def plain_one_per_launch(cloths, device, steps: int, warmup: int, start, budget_s: float = 8.0) -> dict:
+    """The plain FP64 path, one cloth per arena and launch sequence, on the timed
+    frames of the batched run (frames warmup+1 .. warmup+steps, from the batched
+    FP64 run's start state), for a sample of cloths spread over the workload."""
     import torch
 
     from cloth_sim_self_collision_gb300.context import ClothContext
     ctx = ClothContext(device, "fp64")
     stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+    offs = np.concatenate([[0], np.cumsum([3 * c.np for c in cloths])])
+    stride = 37 if len(cloths) % 37 else 41
+    order = [(k * stride) % len(cloths) for k in range(len(cloths))]
     vs, ms, used = 0, 0.0, 0
-    for c in cloths:
+    for i in order:
+        c = cloths[i]
         cid = ctx.add_cloth(c)
-        ctx.step(1)  # builds the arena, first frame untimed
+        ctx.set_states(start[0][offs[i]:offs[i + 1]].copy(), start[1][offs[i]:offs[i + 1]].copy())
         ctx.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        ctx.step(frames)
+        ctx.step(steps)
         e1.record(stream)
         torch.cuda.synchronize()
         ms += e0.elapsed_time(e1)
-        vs += c.np * frames
+        vs += c.np * steps
         used += 1
         ctx.remove_cloth(cid)
         if ms / 1e3 > budget_s:
             break
     ctx.close()
     return {"value": vs / (ms / 1e3), "unit": UNIT,
-            "sample": f"first {used} cloths of the workload, each alone in its own arena (FP64, tree-summed "
-                      f"inner products), frames 2..{frames + 1}"}
+            "sample": f"{used} cloths spread over the workload (every {stride}th), each alone in its own arena "
+                      f"(FP64, tree-summed inner products), on the batched line's timed frames "
+                      f"{warmup + 1}..{warmup + steps} from the batched FP64 run's start state"}
+
+
+def small_config(device: int, frames: int = 300) -> dict:
+    """The reference's own small case (21 x 21 sheet of 1 m over a sphere of
+    radius 0.3, ILU(0)-PCG tol 1e-6, 300 frames) on the plain FP64 GPU path, the
+    oracle restatement of the reference's CPU path timed beside it on one core."""
+    import torch
+
+    from cloth_sim_self_collision_gb300 import scene
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    from oracle import oracle as O
+    c = scene.config_small()
+    ctx = ClothContext(device, "fp64")
+    try:
+        cid = ctx.add_cloth(c)
+        ctx.set_state(cid, c.X0, np.zeros_like(c.X0))
+        stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.step(frames)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gms = e0.elapsed_time(e1)
+    finally:
+        ctx.close()
+    O.build("port")
+    orc = O.OracleCloth(O.OracleLib("port"), c)
+    t0 = time.perf_counter()
+    orc.step(frames)
+    cs = time.perf_counter() - t0
+    return {"workload": f"21x21 sheet, 1 m, z 0.5 over a sphere of radius 0.3, ILU(0)-PCG tol 1e-6, "
+                        f"{frames} frames from rest",
+            "gpu_fp64": {"value": c.np * frames / (gms / 1e3), "ms_per_step": gms / frames},
+            "cpu_port_1core": {"value": c.np * frames / cs, "ms_per_step": 1e3 * cs / frames}}
 
 
 def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, plain_budget_s: float = 40.0) -> dict:
@@ -349,7 +429,7 @@ def native(args):
         # taken at one GPU only
         import torch.distributed as dist
         dist.init_process_group("gloo")
-        args.no_plain = args.no_single = args.no_serve = args.no_cpu = True
+        args.no_plain = args.no_single = args.no_serve = args.no_cpu = args.no_small = True
     B.build()
     torch.cuda.set_device(local)
     cloths = scene.config_batch(count=args.cloths)
@@ -364,15 +444,14 @@ def native(args):
         clocks = ClockSampler(local)
         barrier(world)
         clocks.start()
-        step_ms, prof, counts, launches, start = timed_batch(ctx, ids, args.steps, args.warmup, stream, nv,
-                                                             PROFILED)
+        step_ms, launches, start = timed_batch(ctx, args.steps, args.warmup, stream, nv)
         clk = clocks.stop()
         barrier(world)
         total_ms = max_over_ranks(sum(step_ms), world)
         res = {"value": world * nv * args.steps / (total_ms / 1e3), "ms_per_step": total_ms / args.steps,
                "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
-               "prof": prof, "counts": counts, "launches": launches, "clocks": clk, "nv": nv, "nb": nb_total}
-        if prec == results.get("headline", prec) or not results:
+               "launches": launches, "clocks": clk, "nv": nv, "nb": nb_total, "start": start}
+        if not results:
             # end to end through the C ABI, on the same frames: pinned host state
             # in, frame, state out
             xs = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
@@ -394,12 +473,15 @@ def native(args):
             res["e2e"] = {"value": world * nv * args.steps / (e2e_ms / 1e3), "unit": UNIT,
                           "h2d_bytes_per_step": 2 * 3 * nv * 8, "d2h_bytes_per_step": 2 * 3 * nv * 8}
             results["headline"] = prec
+        # per-kernel times and device counters: a profiled replay of the timed frames
+        res["prof"], res["counts"] = profiled_replay(ctx, args.steps, start, PROFILED)
         results[prec] = res
         ctx.close()
     head = results[results["headline"]]
     plain = None
     if not args.no_plain:
-        plain = plain_one_per_launch(cloths, local, frames=3)
+        st = results["fp64"]["start"] if "fp64" in results else head["start"]
+        plain = plain_one_per_launch(cloths, local, args.steps, args.warmup, st)
 
     # Roofline: the solver kernel (HBM-bound; in mixed precision the persistent inner
     # CG, one launch per refinement cycle) with its algorithmic bytes counted on the
@@ -409,20 +491,32 @@ def native(args):
     top = max(prof, key=lambda k: prof[k][0])
     total_kernel_ms = sum(v[0] for v in prof.values())
     peaks = read_peaks()
+    figs = profile_figures()
     if results["headline"] == "mixed":
         spmv = "mx_persist" if prof["mx_persist"][1] else "mx_spmv"
     else:
         spmv = "cg_spmv"
     ms, n = prof[spmv]
     alg = head["counts"][{"mx_persist": "persist_bytes", "mx_spmv": "spmv32_bytes", "cg_spmv": "spmv64_bytes"}[spmv]]
+    ratio = figs.get((spmv, "dram_per_algorithmic_byte"))
     roof = {"kernel": spmv, "bound": "hbm", "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "peak_source": peaks["source"], "launches": n, "avg_launch_us": 1e3 * ms / max(n, 1),
-            "bytes_per_launch": alg / max(n, 1), "traffic": None,
+            "bytes_per_launch": alg / max(n, 1),
+            "traffic": ratio * alg / max(n, 1) if ratio else None,
+            "traffic_source": (f"ncu dram bytes / algorithmic bytes = {ratio} on a smaller arena "
+                               f"(profiles/), scaled to this run's bytes per launch") if ratio else None,
             "achieved": (alg / max(n, 1)) / (ms / max(n, 1) / 1e3) / 1e9 if ms > 0 else None,
+            "timing": "CUDA events around each launch on the library's stream, in a profiled replay of the "
+                      "timed frames",
             "share_of_kernel_time": ms / total_kernel_ms if total_kernel_ms else None}
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["achieved"] else None
     dominant = {"kernel": top, "share_of_kernel_time": prof[top][0] / total_kernel_ms if total_kernel_ms else None,
                 "launches": prof[top][1], "avg_launch_us": 1e3 * prof[top][0] / max(prof[top][1], 1)}
+    fp64_frac = figs.get((top, "fp64_pipe_active"))
+    if fp64_frac is not None:
+        dominant["bound"] = "fp64 pipe"
+        dominant["fp64_pipe_active_frac"] = fp64_frac
+        dominant["fp64_pipe_source"] = "sm__pipe_fp64_cycles_active from one ncu capture (profiles/)"
 
     if rank != 0:
         return
@@ -432,7 +526,8 @@ def native(args):
         "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if hp == "mixed" else "f64", "data": "synthetic",
-        "config": workload_config(len(cloths), head["nv"], hp),
+        "precision": hp,
+        "config": workload_config(len(cloths), head["nv"]),
         "p50_step_ms": head["p50_step_ms"], "p99_step_ms": head["p99_step_ms"],
         "e2e": head["e2e"], "roofline": roof, "dominant_kernel": dominant,
         "gpu_launches": int(head["launches"]), "clocks": head["clocks"],
@@ -448,6 +543,8 @@ def native(args):
     if plain is not None:
         line["plain_gpu_fp64_one_per_launch"] = plain
         line["vs_plain_gpu"] = head["value"] / plain["value"]
+    if not args.no_small:
+        line["small_21"] = small_config(local)
     if not args.no_single:
         line["single_cloth"] = single_cloths(local)
     if not args.no_serve:
@@ -484,6 +581,7 @@ def reference(args):
     cores, one frame of each per step."""
     import multiprocessing as mp
 
+    from cloth_sim_self_collision_gb300 import scene
     from oracle import oracle as O
     if int(os.environ.get("RANK", "0")) != 0:
         return
@@ -523,7 +621,8 @@ def reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(args.cloths, None, "fp64 (CPU)"),
+        "precision": "fp64 (CPU)",
+        "config": workload_config(args.cloths, workload_vertices(scene.config_batch(count=args.cloths))),
         "p50_step_ms": 1e3 * float(np.percentile(step_s, 50)), "p99_step_ms": 1e3 * float(np.percentile(step_s, 99)),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(groups), "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -545,6 +644,7 @@ def main():
                     help="both: mixed is the headline, FP64 batched reported beside it")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving workload")
     ap.add_argument("--no-single", action="store_true", help="skip the single-cloth configurations")
+    ap.add_argument("--no-small", action="store_true", help="skip the 21x21 ILU(0)-PCG sheet")
     ap.add_argument("--serve-scenes", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, scenes per second")
     ap.add_argument("--serve-steps", type=int, default=200)
