@@ -40,7 +40,8 @@ EXPORTS = [
     "cs_profile", "cs_profile_read", "cs_stream", "cs_profile_bytes", "cs_get_boxes", "cs_solve_cg_noalloc",
     "cs_server_create", "cs_server_submit", "cs_server_wait", "cs_server_release", "cs_server_drain",
     "cs_server_get_stats", "cs_server_last_error", "cs_server_destroy", "cs_scene_device_bytes",
-    "cs_vertex_normals",
+    "cs_vertex_normals", "cs_contact_log", "cs_contact_log_read", "cs_matvec", "cs_set_matrix", "cs_ilu_solve",
+    "cs_distance_fv", "cs_distance_ee", "cs_coplanar_time", "cs_last_residual",
 ]
 
 
@@ -202,6 +203,15 @@ def load(path: str | None = None, build_if_missing: bool = False):
     f("cs_server_destroy", None, _V)
     f("cs_scene_device_bytes", ctypes.c_size_t, i, _D, i, _I, i, _I, P)
     f("cs_vertex_normals", i, _V, i, _D, _D)
+    f("cs_contact_log", i, _V, i)
+    f("cs_matvec", i, _V, i, d, _D, d, _D)
+    f("cs_last_residual", i, _V, i, _D)
+    f("cs_set_matrix", i, _V, i, _D, _D)
+    f("cs_ilu_solve", i, _V, i, _D)
+    f("cs_distance_fv", i, _V, i, _D, _D, _D)
+    f("cs_distance_ee", i, _V, i, _D, _D, _D)
+    f("cs_coplanar_time", i, _V, i, _D, _D, _D)
+    f("cs_contact_log_read", i, _V, i, _I, _I, ctypes.POINTER(ctypes.c_ulonglong), i, _I)
     _lib = L
     return L
 

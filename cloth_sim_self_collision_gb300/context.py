@@ -122,6 +122,24 @@ class ClothContext:
         self._ck(self.L.cs_profile_read(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def log_contacts(self, enable: bool = True):
+        """Record, per detection of each cloth's next contact resolution, (kind,
+        count, digest of the ordered contact list)."""
+        self._ck(self.L.cs_contact_log(self.h, 1 if enable else 0))
+
+    def contact_log(self, cid: int):
+        """The detections of the cloth's last resolution: a list of (ccd, count, digest)."""
+        n = ctypes.c_int()
+        self._ck(self.L.cs_contact_log_read(self.h, cid, None, None, None, 0, ctypes.byref(n)))
+        m = max(n.value, 1)
+        k = np.zeros(m, np.int32)
+        c = np.zeros(m, np.int32)
+        d = np.zeros(m, np.uint64)
+        self._ck(self.L.cs_contact_log_read(self.h, cid, N.ip(k), N.ip(c),
+                                            d.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), m,
+                                            ctypes.byref(n)))
+        return [(int(k[i]), int(c[i]), int(d[i])) for i in range(n.value)]
+
     # ---- stages (host arrays in / out) -------------------------------------------
     def implicit(self, cid, x, v):
         """StepTime_InternalDynamicsILU / StepTime_InternalDynamics (solve_internal_sparse.h:185-326)."""

@@ -348,8 +348,13 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
     A.col32 = m.upload(col32, s);
     A.val32 = m.alloc<float>(vtot);
     CK(cudaMemsetAsync(A.val32, 0, sizeof(float) * (size_t)std::max(vtot, 1LL), s));
-    A.dinv32 = m.alloc<float>(9 * (size_t)NV);
+    A.linv32 = m.alloc<float>(9 * (size_t)NV);
     A.r32 = m.alloc<float>(3 * (size_t)NV);
+    A.r32b = m.alloc<float>(3 * (size_t)NV);
+    A.w32 = m.alloc<float>(3 * (size_t)NV);
+    A.w32b = m.alloc<float>(3 * (size_t)NV);
+    A.s32 = m.alloc<float>(3 * (size_t)NV);
+    A.s32b = m.alloc<float>(3 * (size_t)NV);
     A.d32 = m.alloc<float>(3 * (size_t)NV);
     A.p32 = m.alloc<float>(3 * (size_t)NV);
     A.q32 = m.alloc<float>(3 * (size_t)NV);
@@ -369,7 +374,8 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
     A.red_cnt = m.alloc<int>(std::max(ni, 1));
     CK(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(ni, 1), s));
     // persistent inner solve: algorithmic bytes of one iteration over a slice
-    // (blocks and columns; p_prev, z, p, q in phase A; d, p, q, r, D^-1, z in phase B)
+    // (blocks and columns; r, w, s_prev, p_prev and d read; s, r_next, w_next, p
+    // and d written)
     {
       std::vector<long long> pb(A.nslice, 0);
       for (int k = 0; k < A.nslice; k++) {
@@ -377,11 +383,9 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
         const ClothTopo& t = cl[i]->topo;
         const int r0 = slice_row0[k] - o.voff[i];
         for (int l = 0; l < 32 && r0 + l < t.np; l++)
-          pb[k] += 40LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l] + 1) + 168;
+          pb[k] += 40LL * (t.row_ptr[r0 + l + 1] - t.row_ptr[r0 + l] + 1) + 120;
       }
       A.slice_pbytes = m.upload(pb, s);
-
-      A.p32b = m.alloc<float>(3 * (size_t)NV);
       A.dg_range = m.alloc<unsigned>(2 * (size_t)std::max(ni, 1));
       A.grid_bar = m.alloc<unsigned int>(4);
       CK(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s));
@@ -453,8 +457,9 @@ std::vector<int> live(const cs_ctx* c, const std::vector<int>& act) {
 }
 
 void set_active(cs_ctx* c, const std::vector<int>& act) {
-  const std::vector<int> a = live(c, act);
-  CK(cudaMemcpyAsync(c->A.active, a.data(), sizeof(int) * a.size(), cudaMemcpyHostToDevice, c->stream));
+  c->cur_act = live(c, act);
+  CK(cudaMemcpyAsync(c->A.active, c->cur_act.data(), sizeof(int) * c->cur_act.size(), cudaMemcpyHostToDevice,
+                     c->stream));
 }
 
 // cloths whose broad phase flagged them as blown up stop here
@@ -583,6 +588,39 @@ void implicit(cs_ctx* c, const std::vector<int>& act) {
 constexpr long long kMaxPairs = 1LL << 28;
 constexpr long long kMaxCandidates = 1LL << 25;
 
+// FNV-1a over the 32-bit words of an ordered contact list (5 words a contact,
+// cloth-local vertex ids), the digest of the contact log
+unsigned long long contact_digest(const int* ce, long long n) {
+  unsigned long long d = 14695981039346656037ULL;
+  for (long long i = 0; i < 5 * n; i++) {
+    d ^= (unsigned long long)(unsigned)ce[i];
+    d *= 1099511628211ULL;
+  }
+  return d;
+}
+
+// appends the last detection's ordered contact list of every active cloth to
+// the contact log (host copies: a test facility, off by default)
+void log_detection(cs_ctx* c, int ccd, int total) {
+  const int ni = c->A.ni;
+  std::vector<int> lo(ni);
+  std::vector<int> ce(5 * (size_t)std::max(total, 1));
+  CK(cudaMemcpyAsync(lo.data(), c->C.ce_inst_lo, sizeof(int) * ni, cudaMemcpyDeviceToHost, c->stream));
+  if (total > 0)
+    CK(cudaMemcpyAsync(ce.data(), c->C.ce, sizeof(int) * 5 * (size_t)total, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < ni; i++) {
+    if (i >= (int)c->cur_act.size() || !c->cur_act[i]) continue;
+    const int n = c->hst[i].n_contacts, vo = c->voff[i];
+    std::vector<int> loc(5 * (size_t)std::max(n, 1));
+    for (int e = 0; e < n; e++) {
+      loc[5 * e] = ce[5 * ((size_t)lo[i] + e)];
+      for (int k = 1; k < 5; k++) loc[5 * e + k] = ce[5 * ((size_t)lo[i] + e) + k] - vo;
+    }
+    c->clog[c->order[i]].push_back({ccd, n, contact_digest(loc.data(), n)});
+  }
+}
+
 // detection for the active cloths; returns the total number of contacts and
 // leaves per-cloth counts in c->hst.  incremental (CCD only): the previous
 // detection's candidates are kept for pairs without a dirty triangle and only
@@ -621,6 +659,7 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
       prof_count("detections", 1);
       c->last_ncand = ncand;
       c->last_nce = total;
+      if (c->log_on) log_detection(c, ccd, total);
       return total;
     }
     // a buffer overflowed: fall back to a full detection (which grows the buffers)
@@ -677,6 +716,7 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
   prof_count("detections", 1);
   c->last_ncand = ncand;
   c->last_nce = total;
+  if (c->log_on) log_detection(c, ccd, total);
   return total;
 }
 
@@ -699,6 +739,7 @@ std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
   std::vector<int> applied(ni, 0), phase = act;
   for (int i = 0; i < ni; i++)
     if (act[i]) {
+      if (c->log_on) c->clog[c->order[i]].clear();
       cs_stats& st = c->cloths[c->order[i]]->stats;
       const int it = st.solver_iterations, sing = st.ilu_singular;
       const double conv = st.solver_conv;
@@ -1196,6 +1237,56 @@ int cs_spmv(cs_ctx* c, int id, const double* x, double* y) {
   });
 }
 
+int cs_last_residual(cs_ctx* c, int id, double* r) {
+  return guarded(c, [&] {
+    if (!r) throw ArgError("null vector");
+    ensure(c);
+    const int i = slot_of(c, id);
+    down(c, r, c->A.r + 3 * (size_t)c->voff[i], 3 * (size_t)c->cloths[id]->topo.np);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_set_matrix(cs_ctx* c, int id, const double* vdia, const double* vcrs) {
+  return guarded(c, [&] {
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    if (vdia) up(c, c->A.vdia + 9 * (size_t)c->voff[i], vdia, 9 * (size_t)t.np);
+    if (vcrs) up(c, c->A.vcrs + 9 * (size_t)c->boff[i], vcrs, 9 * (size_t)t.nb);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_matvec(cs_ctx* c, int id, double alpha, const double* x, double beta, double* y) {
+  return guarded(c, [&] {
+    if (!x || !y) throw ArgError("null vector");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const size_t n = 3 * (size_t)c->cloths[id]->topo.np;
+    up(c, c->A.p + 3 * (size_t)c->voff[i], x, n);
+    up(c, c->A.z + 3 * (size_t)c->voff[i], y, n);
+    launch_matvec(c->A, c->voff[i], c->voff[i + 1], alpha, c->A.p, beta, c->A.z, c->stream);
+    down(c, y, c->A.z + 3 * (size_t)c->voff[i], n);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int cs_ilu_solve(cs_ctx* c, int id, double* vec) {
+  return guarded(c, [&] {
+    if (!vec) throw ArgError("null vector");
+    ensure(c);
+    const int i = slot_of(c, id);
+    const ClothTopo& t = c->cloths[id]->topo;
+    if (t.lev_ptr.empty()) throw ArgError("cloth was added without the ILU(0) solver");
+    const size_t n = 3 * (size_t)t.np;
+    up(c, c->A.z + 3 * (size_t)c->voff[i], vec, n);
+    launch_ilu_solve(c->A, i, c->A.z, c->stream);
+    down(c, vec, c->A.z + 3 * (size_t)c->voff[i], n);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
 int cs_bvh_nodes(cs_ctx* c, int id, int* nnode, int* nodes) {
   return guarded(c, [&] {
     const ClothTopo& t = cloth_at(c, id).topo;
@@ -1476,6 +1567,49 @@ int cs_element_contact(cs_ctx* c, int n, const double* cc, const cs_params* prm,
                        [&](std::vector<double*>& i, std::vector<double*>& o) {
                          launch_element_batch_contact(n, i[0], &d, o[0], o[1], o[2], c->stream);
                        });
+}
+
+int cs_distance_fv(cs_ctx* c, int n, const double* pts, double* dist, double* w) {
+  return element_batch(c, n, {{pts, 12}}, {{dist, 1}, {w, 2}},
+                       [&](std::vector<double*>& i, std::vector<double*>& o) {
+                         launch_distance_fv(n, i[0], o[0], o[1], c->stream);
+                       });
+}
+
+int cs_distance_ee(cs_ctx* c, int n, const double* pts, double* dist, double* ratio) {
+  return element_batch(c, n, {{pts, 12}}, {{dist, 1}, {ratio, 2}},
+                       [&](std::vector<double*>& i, std::vector<double*>& o) {
+                         launch_distance_ee(n, i[0], o[0], o[1], c->stream);
+                       });
+}
+
+int cs_coplanar_time(cs_ctx* c, int n, const double* s0, const double* e0, double* t) {
+  return element_batch(c, n, {{s0, 12}, {e0, 12}}, {{t, 1}},
+                       [&](std::vector<double*>& i, std::vector<double*>& o) {
+                         launch_coplanar_time(n, i[0], i[1], o[0], c->stream);
+                       });
+}
+
+int cs_contact_log(cs_ctx* c, int enable) {
+  return guarded(c, [&] {
+    c->log_on = enable != 0;
+    c->clog.clear();
+  });
+}
+
+int cs_contact_log_read(cs_ctx* c, int id, int* kind, int* count, unsigned long long* digest, int cap, int* n) {
+  return guarded(c, [&] {
+    if (!c->cloths.count(id)) throw ArgError("unknown cloth id");
+    const auto it = c->clog.find(id);
+    const int m = it == c->clog.end() ? 0 : (int)it->second.size();
+    if (n) *n = m;
+    for (int e = 0; e < m && e < cap; e++) {
+      if (kind) kind[e] = it->second[e].kind;
+      if (count) count[e] = it->second[e].count;
+      if (digest) digest[e] = it->second[e].digest;
+    }
+    if (m > cap && (kind || count || digest)) throw CapacityError("contact log longer than cap");
+  });
 }
 
 long long cs_launch_count(const cs_ctx* c) { return c ? g_launches - c->launches0 : 0; }

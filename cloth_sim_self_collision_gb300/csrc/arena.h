@@ -50,12 +50,13 @@ struct InstState {
   int total_iters;   // inner iterations summed over refinement cycles
   int cycles;        // refinement cycles
   double red[3];     // per-cloth totals of the slice partials: p.q, r.z, r.r
-  // persistent inner solve: r.z of the iterations by parity; istop is set at
-  // the end of phase B when the cloth converges (no block reads it before the
+  // persistent inner solve (single-reduction CG): gamma = r.r of the current
+  // iteration and alpha (FP64 copies for the recurrence); istop is set at the
+  // end of an iteration when the cloth converges (no block reads it before the
   // barrier that follows); alpha and beta as the cloth's last block left them
-  double rzh[2];
+  double gam, alf;
   int istop;
-  int bjac;          // the inner solve applies block-Jacobi (else no preconditioner)
+  int bjac;          // the inner solve runs on the block-Jacobi-scaled matrix
   float alpha32, beta32;
 };
 
@@ -110,9 +111,16 @@ struct Arena {
   long long* sell_pos = nullptr;    // per slot (off-diagonal then diagonal): value offset of entry 0
   float* val32 = nullptr;
   int* col32 = nullptr;
-  float* dinv32 = nullptr;          // 9 per vertex
+  // block-Jacobi scaling: L^-1 of the Cholesky factor of each diagonal block
+  // (lower triangular, 9 per vertex; identity where the block is not positive
+  // definite).  Cloths that use it have their FP32 matrix scaled once per frame
+  // to S A S^T (S = blockdiag(L^-1)), on which CG is block-Jacobi PCG.
+  float* linv32 = nullptr;
   float *r32 = nullptr, *d32 = nullptr, *p32 = nullptr, *q32 = nullptr, *z32 = nullptr;
-  double* part32 = nullptr;         // 3 per slice: p.q, r.z, r.r
+  // single-reduction CG of the persistent solve: residual, A * residual and
+  // A * direction, each double-buffered by iteration parity
+  float *r32b = nullptr, *w32 = nullptr, *w32b = nullptr, *s32 = nullptr, *s32b = nullptr;
+  double* part32 = nullptr;         // 3 per slice: inner-product partials
   int* red_cnt = nullptr;           // per cloth: slices that have written their partials
   // algorithmic bytes of one SpMV over a slice / chunk (real blocks, column
   // indices, x once, y once) and their running totals while profiling
@@ -122,11 +130,9 @@ struct Arena {
                                             // tests reaching FP64: FV prx, EE prx, FV ccd, EE ccd
   int count_bytes = 0;
   int mixed = 0;                    // mixed-precision arrays present
-  // persistent inner solve: a second direction buffer (the direction is built on
-  // the fly from the previous one), per-slice algorithmic bytes of one iteration,
-  // and the grid barrier state
+  // persistent inner solve: per-slice algorithmic bytes of one iteration and
+  // the grid barrier state
   long long* slice_pbytes = nullptr;
-  float* p32b = nullptr;
   // per cloth: smallest and largest diagonal entry of the assembled matrix (as
   // the bits of positive floats) for the choice of preconditioner
   unsigned* dg_range = nullptr;

@@ -113,6 +113,15 @@ struct cs_ctx {
   int mx_cap = 300;
   // per slot: the cloth blew up (CS_ERR_DIVERGED) and is no longer stepped
   std::vector<int> dead;
+  // slots of the last set_active (cloths that the next launches touch)
+  std::vector<int> cur_act;
+  // contact log (cs_contact_log): per cloth id, one entry per detection of its last resolve
+  struct LogEntry {
+    int kind, count;
+    unsigned long long digest;
+  };
+  bool log_on = false;
+  std::map<int, std::vector<LogEntry>> clog;
 };
 
 namespace cs {

@@ -363,6 +363,46 @@ __device__ __forceinline__ bool ccd_no_root32(V3<double> x1d, V3<double> x2d, V3
   return pos || neg;
 }
 
+// a . b with its error bound, for FP32 vectors with per-component error bounds
+__device__ __forceinline__ void f3e_dot(const F3E& a, const F3E& b, float& t, float& e) {
+  const float u = 5.9604645e-8f;
+  float s = 0.f, r = 0.f, mm = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float p = a.v[k] * b.v[k];
+    s = s + p;
+    r += (fabsf(a.v[k]) + a.e[k]) * b.e[k] + fabsf(b.v[k]) * a.e[k];
+    mm += fabsf(p);
+  }
+  t = s;
+  e = 1.001f * (r + 3.1f * u * mm);
+}
+
+// True when the coplanarity-sign rejection of IsContact_FV_CCD
+// (bvh_aabb.cpp:683-690, the first block of fv_ccd) certainly fires: with the
+// start normal n = (p1 - p0) x (p2 - p0), the four signed heights
+// (p0 - p3).n, (q0 - q3).n, (q1 - q3).n, (q2 - q3).n have one sign.  The
+// differences arrive as FP64 values (rounded here to FP32, 2^-24 relative);
+// every product and sum carries an error bound, and each height must clear
+// twice its bound (which covers the FP64 evaluation's own rounding) and a floor
+// of 1e-30, so the FP64 products t0 * ti are nonzero with the same sign.
+__device__ __forceinline__ bool fv_sign_reject32(V3<double> e1, V3<double> e2, V3<double> h0, V3<double> h1,
+                                                 V3<double> h2, V3<double> h3) {
+  const F3E n = f3e_cross(f3e_round(e1), f3e_round(e2));
+  float t[4], e[4];
+  f3e_dot(f3e_round(h0), n, t[0], e[0]);
+  f3e_dot(f3e_round(h1), n, t[1], e[1]);
+  f3e_dot(f3e_round(h2), n, t[2], e[2]);
+  f3e_dot(f3e_round(h3), n, t[3], e[3]);
+  bool pos = true, neg = true;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    pos = pos && t[k] - 2.0f * e[k] > 1.0e-30f;
+    neg = neg && t[k] + 2.0f * e[k] < -1.0e-30f;
+  }
+  return pos || neg;
+}
+
 // ---------------------------------------------------------------------------
 // elementary contact tests (bvh_aabb.cpp:392-438, 666-793)
 // ---------------------------------------------------------------------------

@@ -177,24 +177,33 @@ __global__ void k_slot_reduce(Arena A) {
       atomicMin(&A.dg_range[2 * inst], __float_as_uint(lo));
       atomicMax(&A.dg_range[2 * inst + 1], __float_as_uint(hi));
     }
-    // block-Jacobi preconditioner: inverse of the diagonal block (identity if singular)
-    const double det = acc[0] * (acc[4] * acc[8] - acc[5] * acc[7]) - acc[1] * (acc[3] * acc[8] - acc[5] * acc[6]) +
-                       acc[2] * (acc[3] * acc[7] - acc[4] * acc[6]);
-    float* D = A.dinv32 + 9 * (size_t)v;
-    if (fabs(det) > 1e-300) {
-      const double r = 1.0 / det;
-      D[0] = (float)(r * (acc[4] * acc[8] - acc[5] * acc[7]));
-      D[1] = (float)(r * (acc[2] * acc[7] - acc[1] * acc[8]));
-      D[2] = (float)(r * (acc[1] * acc[5] - acc[2] * acc[4]));
-      D[3] = (float)(r * (acc[5] * acc[6] - acc[3] * acc[8]));
-      D[4] = (float)(r * (acc[0] * acc[8] - acc[2] * acc[6]));
-      D[5] = (float)(r * (acc[2] * acc[3] - acc[0] * acc[5]));
-      D[6] = (float)(r * (acc[3] * acc[7] - acc[4] * acc[6]));
-      D[7] = (float)(r * (acc[1] * acc[6] - acc[0] * acc[7]));
-      D[8] = (float)(r * (acc[0] * acc[4] - acc[1] * acc[3]));
+    // block-Jacobi scaling: L^-1 for the Cholesky factor D = L L^T of the
+    // diagonal block (lower triangle of D), identity unless D is positive definite
+    float* S = A.linv32 + 9 * (size_t)v;
+    const double l00 = sqrt(acc[0]);
+    const double l10 = acc[3] / l00, l20 = acc[6] / l00;
+    const double t11 = acc[4] - l10 * l10;
+    const double l11 = sqrt(t11);
+    const double l21 = (acc[7] - l20 * l10) / l11;
+    const double t22 = acc[8] - l20 * l20 - l21 * l21;
+    const double l22 = sqrt(t22);
+    if (acc[0] > 0.0 && t11 > 0.0 && t22 > 0.0 && isfinite(l22) && isfinite(l21)) {
+      const double m00 = 1.0 / l00, m11 = 1.0 / l11, m22 = 1.0 / l22;
+      const double m10 = -l10 * m00 * m11;
+      const double m21 = -l21 * m11 * m22;
+      const double m20 = -(l20 * m00 + l21 * m10) * m22;
+      S[0] = (float)m00;
+      S[1] = 0.f;
+      S[2] = 0.f;
+      S[3] = (float)m10;
+      S[4] = (float)m11;
+      S[5] = 0.f;
+      S[6] = (float)m20;
+      S[7] = (float)m21;
+      S[8] = (float)m22;
     } else {
 #pragma unroll
-      for (int k = 0; k < 9; k++) D[k] = (k % 4 == 0) ? 1.f : 0.f;
+      for (int k = 0; k < 9; k++) S[k] = (k % 4 == 0) ? 1.f : 0.f;
     }
   }
 }

@@ -455,18 +455,30 @@ __global__ void k_narrow_fv(Arena A, ContactBufs C, int ccd, const double* xs, c
     const bool fa = test < 3;
     const int tf = fa ? ta : tb, tv = fa ? tb : ta, k = fa ? test : test - 3;
     const int f0 = A.tri[3 * tf], f1 = A.tri[3 * tf + 1], f2 = A.tri[3 * tf + 2], q = A.tri[3 * tv + k];
-    count_fp64_test(A, ccd ? 4 : 2);
     const V3<double> p0 = ld3(xs, f0), p1 = ld3(xs, f1), p2 = ld3(xs, f2), p3 = ld3(xs, q);
     if (!ccd) {
+      count_fp64_test(A, 2);
       // the reference passes aBB[triangle index]: the box of the node whose
       // index equals the triangle's index within its cloth
       const Box bb = A.box[A.noff[inst] + (tf - A.toff[inst])];
       if (fv_proximity(f0, f1, f2, q, p0, p1, p2, p3, bb, delta)) emit(C, 1, f0, f1, f2, q, na, nb, test);
     } else {
+      const V3<double> q0 = end_pos(xs, vs, f0, P.dt), q1 = end_pos(xs, vs, f1, P.dt);
+      const V3<double> q2 = end_pos(xs, vs, f2, P.dt), q3 = end_pos(xs, vs, q, P.dt);
+      {
+        // FP32 certificates that the FP64 test rejects: the vertex stays on one
+        // side of the start face plane (the test's sign block), or the four
+        // points are never coplanar in [0, 1] (FindCoplanerInterp returns -1);
+        // both from the FP64 differences the FP64 test itself forms
+        const V3<double> x1 = p1 - p0, x2 = p2 - p0;
+        if (fv_sign_reject32(x1, x2, p0 - p3, q0 - q3, q1 - q3, q2 - q3)) continue;
+        const V3<double> x3 = p3 - p0;
+        const V3<double> v1 = (q1 - q0) - x1, v2 = (q2 - q0) - x2, v3 = (q3 - q0) - x3;
+        if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
+      }
+      count_fp64_test(A, 4);
       const Box bb = A.box[fa ? na : nb];
-      if (fv_ccd(f0, f1, f2, q, p0, p1, p2, p3, end_pos(xs, vs, f0, P.dt), end_pos(xs, vs, f1, P.dt),
-                 end_pos(xs, vs, f2, P.dt), end_pos(xs, vs, q, P.dt), bb))
-        emit(C, 1, f0, f1, f2, q, na, nb, test);
+      if (fv_ccd(f0, f1, f2, q, p0, p1, p2, p3, q0, q1, q2, q3, bb)) emit(C, 1, f0, f1, f2, q, na, nb, test);
     }
   }
 }
@@ -1063,6 +1075,56 @@ void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double
   k_impulse_apply<<<A.ni, 128, 0, s>>>(A, C, ccd, xs, vs);
   prof_end(PK_IMPULSE, s);
   g_launches += 2;
+}
+
+namespace {
+__device__ __forceinline__ V3<double> pt(const double* a, int k) { return V3<double>{a[3 * k], a[3 * k + 1], a[3 * k + 2]}; }
+
+// DistanceFaceVertex (bvh_aabb.cpp:321-340) per item: face p0 p1 p2, vertex p3
+__global__ void k_distance_fv(int n, const double* pts, double* dist, double* w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* a = pts + 12 * (size_t)i;
+  double w0, w1;
+  dist[i] = dist_face_vertex(pt(a, 0), pt(a, 1), pt(a, 2), pt(a, 3), w0, w1);
+  w[2 * i] = w0;
+  w[2 * i + 1] = w1;
+}
+
+// DistanceEdgeEdge (bvh_aabb.cpp:343-384) per item: edges p0 p1 and q0 q1
+__global__ void k_distance_ee(int n, const double* pts, double* dist, double* ratio) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* a = pts + 12 * (size_t)i;
+  double rp, rq;
+  dist[i] = dist_edge_edge(pt(a, 0), pt(a, 1), pt(a, 2), pt(a, 3), rp, rq);
+  ratio[2 * i] = rp;
+  ratio[2 * i + 1] = rq;
+}
+
+// FindCoplanerInterp (bvh_aabb.cpp:598-662) per item: start and end points
+__global__ void k_coplanar_time(int n, const double* s0, const double* e0, double* t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* a = s0 + 12 * (size_t)i;
+  const double* b = e0 + 12 * (size_t)i;
+  t[i] = coplanar_time(pt(a, 0), pt(a, 1), pt(a, 2), pt(a, 3), pt(b, 0), pt(b, 1), pt(b, 2), pt(b, 3));
+}
+}  // namespace
+
+void launch_distance_fv(int n, const double* pts, double* dist, double* w, cudaStream_t s) {
+  k_distance_fv<<<nblk(n), kT, 0, s>>>(n, pts, dist, w);
+  g_launches++;
+}
+
+void launch_distance_ee(int n, const double* pts, double* dist, double* ratio, cudaStream_t s) {
+  k_distance_ee<<<nblk(n), kT, 0, s>>>(n, pts, dist, ratio);
+  g_launches++;
+}
+
+void launch_coplanar_time(int n, const double* s0, const double* e0, double* t, cudaStream_t s) {
+  k_coplanar_time<<<nblk(n), kT, 0, s>>>(n, s0, e0, t);
+  g_launches++;
 }
 
 void launch_riz_reset(const Arena& A, cudaStream_t s) {

@@ -58,30 +58,22 @@ __device__ void finish_cloth(const Arena& A, int inst, int lane, int f0, int nf)
   if (lane == 0) A.red_cnt[inst] = 0;
 }
 
-__device__ __forceinline__ void precondition(const Arena& A, int bjac, int row, const float r[3], float z[3]);
-
 // Preconditioner choice per cloth and frame: block-Jacobi when the diagonal's
 // entries spread by more than kJacobiSpread (obstacle contact terms), else none
 // (CG as the reference's Solve_CG).  Without contact the right-hand side of a
 // falling sheet is close to a rigid translation, an eigenvector of M/dt^2 + K,
 // which unpreconditioned CG resolves in a few iterations and the boundary-varying
 // Jacobi scaling does not; with contact terms block-Jacobi converges faster.
+// Block-Jacobi is applied as a symmetric scaling: with D_i = L_i L_i^T (Cholesky
+// of the diagonal block) and S = blockdiag(L_i^-1), CG on S A S^T y = S r,
+// d = S^T y is block-Jacobi PCG, and the inner loop carries no preconditioner.
 constexpr float kJacobiSpread = 10.0f;
 
-__device__ __forceinline__ void apply_dinv(const float* D, const float r[3], float z[3]) {
-  z[0] = D[0] * r[0] + D[1] * r[1] + D[2] * r[2];
-  z[1] = D[3] * r[0] + D[4] * r[1] + D[5] * r[2];
-  z[2] = D[6] * r[0] + D[7] * r[1] + D[8] * r[2];
-}
-
-__device__ __forceinline__ void precondition(const Arena& A, int bjac, int row, const float r[3], float z[3]) {
-  if (bjac) {
-    apply_dinv(A.dinv32 + 9 * (size_t)row, r, z);
-  } else {
-    z[0] = r[0];
-    z[1] = r[1];
-    z[2] = r[2];
-  }
+// y = L^-1 x, with L^-1 lower triangular (row-major 3x3)
+__device__ __forceinline__ void apply_l(const float* S, const float x[3], float y[3]) {
+  y[0] = S[0] * x[0];
+  y[1] = S[3] * x[0] + S[4] * x[1];
+  y[2] = S[6] * x[0] + S[7] * x[1] + S[8] * x[2];
 }
 
 struct SliceCtx {
@@ -102,32 +94,70 @@ __device__ __forceinline__ bool slice_ctx(const Arena& A, SliceCtx& c, bool need
   return true;
 }
 
-// r32 = r (FP64 residual), d = 0, z = D^-1 r, p = z; slice partials of r.z and r.r
+// FP32 matrix of the cloths that use block-Jacobi: each block A_ij becomes
+// L_i^-1 A_ij L_j^-T (once per frame, after the preconditioner choice)
+__global__ void __launch_bounds__(kSliceThreads) k_mx_scale(Arena A) {
+  SliceCtx c;
+  if (!slice_ctx(A, c, false) || !A.st[c.inst].bjac || !c.valid) return;
+  const int w = A.slice_w[c.slice];
+  float* V = A.val32 + A.slice_voff[c.slice] + c.lane;
+  const int* Cc = A.col32 + A.slice_coff[c.slice] + c.lane;
+  float Si[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) Si[k] = A.linv32[9 * (size_t)c.row + k];
+  for (int j = 0; j < w; j++) {
+    const int col = Cc[32 * j];
+    float Sj[9], B[9], T[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      Sj[k] = A.linv32[9 * (size_t)col + k];
+      B[k] = V[288 * j + 32 * k];
+    }
+    // T = B L_j^-T: T[a][b] = sum_c B[a][c] Sj[b][c]
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) T[3 * a + b] = B[3 * a + 0] * Sj[3 * b + 0] + B[3 * a + 1] * Sj[3 * b + 1] +
+                                                 B[3 * a + 2] * Sj[3 * b + 2];
+    // L_i^-1 T
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+        V[288 * j + 32 * (3 * a + b)] = Si[3 * a + 0] * T[b] + Si[3 * a + 1] * T[3 + b] + Si[3 * a + 2] * T[6 + b];
+  }
+}
+
+// r32 = S r (scaled cloths) or r, from the FP64 residual; d = 0, z = p = r32;
+// slice partials of r.r (fields 1 and 2: r.z equals r.r without a preconditioner)
 __global__ void __launch_bounds__(kSliceThreads) k_mx_inner_init(Arena A) {
   SliceCtx c;
   if (!slice_ctx(A, c, false)) return;
-  float rz = 0.f, rr = 0.f;
+  float rr = 0.f;
   if (c.valid) {
-    float r[3], z[3];
+    float r[3];
+    if (A.st[c.inst].bjac) {
+      const float* S = A.linv32 + 9 * (size_t)c.row;
+      const double r0 = A.r[3 * c.row], r1 = A.r[3 * c.row + 1], r2 = A.r[3 * c.row + 2];
+      r[0] = (float)((double)S[0] * r0);
+      r[1] = (float)((double)S[3] * r0 + (double)S[4] * r1);
+      r[2] = (float)((double)S[6] * r0 + (double)S[7] * r1 + (double)S[8] * r2);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 3; k++) r[k] = (float)A.r[3 * c.row + k];
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      r[k] = (float)A.r[3 * c.row + k];
       A.r32[3 * c.row + k] = r[k];
       A.d32[3 * c.row + k] = 0.f;
-    }
-    precondition(A, A.st[c.inst].bjac, c.row, r, z);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      A.z32[3 * c.row + k] = z[k];
-      A.p32[3 * c.row + k] = z[k];
-      rz += r[k] * z[k];
+      A.z32[3 * c.row + k] = r[k];
+      A.p32[3 * c.row + k] = r[k];
       rr += r[k] * r[k];
     }
   }
-  rz = warp_sum_f(rz);
   rr = warp_sum_f(rr);
   if (c.lane == 0) {
-    A.part32[3 * c.slice + 1] = rz;
+    A.part32[3 * c.slice + 1] = rr;
     A.part32[3 * c.slice + 2] = rr;
   }
 }
@@ -176,7 +206,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_spmv(Arena A) {
   finish_cloth(A, c.inst, c.lane, 0, 1);
 }
 
-// alpha = r.z / p.q; d += alpha p; r -= alpha q; z = D^-1 r; partials of r.z, r.r
+// alpha = r.z / p.q; d += alpha p; r -= alpha q; z = r; partials of r.z, r.r
 __global__ void __launch_bounds__(kSliceThreads) k_mx_update(Arena A, int it) {
   SliceCtx c;
   if (!slice_ctx(A, c, true)) return;
@@ -192,9 +222,9 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_update(Arena A, int it) {
       r[k] = fmaf(-alpha, A.q32[i], A.r32[i]);
       A.r32[i] = r[k];
     }
-    precondition(A, A.st[c.inst].bjac, c.row, r, z);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
+      z[k] = r[k];
       A.z32[3 * c.row + k] = z[k];
       rz += r[k] * z[k];
       rr += r[k] * r[k];
@@ -239,25 +269,32 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
 
 // ---- persistent inner solve ---------------------------------------------------------
 // One cooperative launch runs every inner CG iteration of a refinement cycle for
-// all cloths.  Per iteration, two phases separated by grid barriers:
-//   A: p = z + beta p_prev is built on the fly (for the rows a slice reads and
-//      for its own rows, which it stores), q = A32 p, and the slice partials
-//      of p.q; the last block to finish a cloth's slices sums its partials and
-//      stores alpha = r.z / p.q.
-//   B: d += alpha p, r -= alpha q, z = D^-1 r, and the slice partials of r.z
-//      and r.r; the last block to finish a cloth's slices sums them and decides
-//      convergence (|r|^2 <= eta^2 |r0|^2, or the cap) or stores beta.
-// "Last block" is a per-cloth ticket counted in slices, so each total is
-// summed once, in slice order by a block of fixed size: results depend neither
-// on the launch shape nor on the other cloths.  A converged cloth sets istop and
-// decrements the count of cloths still iterating; all blocks read that count
-// after the barrier that ends phase B (nothing changes it before the next
-// phase B), so they leave the loop together.
+// all cloths, in the single-reduction form of CG (Chronopoulos and Gear, 1989:
+// "s-step iterative methods for symmetric linear systems", J. Comput. Appl.
+// Math. 25): with w = A r and s = A p carried by recurrence, both inner
+// products of an iteration are taken together, so an iteration is one phase
+// and one grid barrier.  Iteration i (alpha_i, beta_i from the previous one):
+//   s_i = w_i + beta_i s_{i-1},  p_i = r_i + beta_i p_{i-1},  d += alpha_i p_i,
+//   r_{i+1} = r_i - alpha_i s_i,  w_{i+1} = A r_{i+1},
+//   gamma_{i+1} = r_{i+1}.r_{i+1},  delta_{i+1} = w_{i+1}.r_{i+1},
+//   beta_{i+1} = gamma_{i+1} / gamma_i,
+//   alpha_{i+1} = gamma_{i+1} / (delta_{i+1} - beta_{i+1} gamma_{i+1} / alpha_i).
+// The SpMV needs r_{i+1} at the neighbour rows, which other blocks update in the
+// same phase: it recomputes them from r_i, w_i and s_{i-1} with the same fused
+// operations the owning row uses, so both agree bit for bit.  r, w and s are
+// double-buffered by parity; p and d are read only by their own row.
+// Block-Jacobi cloths run on the scaled matrix, so no preconditioner appears.
+// Totals: the block whose slices complete a cloth (a per-cloth ticket counted in
+// slices) sums the cloth's partials in slice order with a block of fixed size,
+// so results depend neither on the launch shape nor on the other cloths; it
+// decides convergence (|r|^2 <= eta^2 |r0|^2, or the cap) or stores alpha and
+// beta.  A converged cloth sets istop and decrements the count of cloths still
+// iterating; all blocks read that count after the barrier that ends the
+// iteration, so they leave the loop together.
 // Work split: the slices of the cloths still iterating, in arena order, are cut
 // into one contiguous range per block, re-cut whenever a cloth stops, so blocks
 // do not idle on converged cloths (arenas of more than kRebalanceMax cloths
-// keep the static cut over all slices and skip converged cloths).  The
-// direction buffers alternate between iterations.
+// keep the static cut over all slices and skip converged cloths).
 constexpr unsigned kSpinLimit = 1u << 22;  // ~1 s of polling at the least
 constexpr int kRebalanceMax = 2048;        // cloths whose slice prefix fits in shared memory
 
@@ -434,15 +471,21 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads) k_mx_
       compact_range<kPersistThreads>(A, s_pref, s_wsum, R);
       cut_at = left;
     }
-    const float* Pold = (it & 1) ? A.p32 : A.p32b;
-    float* Pnew = (it & 1) ? A.p32b : A.p32;
-    // ---- phase A: direction, SpMV, p.q
+    // iteration 1 reads r_1, w_1 from r32, w32 (the start kernels) and no s, p
+    const bool odd = (it & 1) != 0;
+    const float* Rc = odd ? A.r32 : A.r32b;
+    const float* Wc = odd ? A.w32 : A.w32b;
+    const float* Sp = odd ? A.s32b : A.s32;
+    float* Rn = odd ? A.r32b : A.r32;
+    float* Wn = odd ? A.w32b : A.w32;
+    float* Sn = odd ? A.s32 : A.s32b;
+    const bool first = it == 1;
     for (int inst = R.c0; inst <= R.c1; inst++) {
       int lo, hi;
       if (!portion(A, R, compact, s_pref, inst, lo, hi)) continue;
       const InstState& St = A.st[inst];
-      const float beta = it > 1 ? St.beta32 : 0.f;
-      const int bjac = St.bjac;
+      const float alpha = St.alpha32;
+      const float beta = first ? 0.f : St.beta32;
       for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
         const int row = A.slice_row0[sl] + lane;
         const int w = A.slice_w[sl];
@@ -452,91 +495,63 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads) k_mx_
 #pragma unroll 2
         for (int j = 0; j < w; j++) {
           const int col = Cc[32 * j];
-          const float x0 = fmaf(beta, Pold[3 * col + 0], A.z32[3 * col + 0]);
-          const float x1 = fmaf(beta, Pold[3 * col + 1], A.z32[3 * col + 1]);
-          const float x2 = fmaf(beta, Pold[3 * col + 2], A.z32[3 * col + 2]);
-          const float* v = V + 288 * j;
-          y0 = fmaf(v[0], x0, fmaf(v[32], x1, fmaf(v[64], x2, y0)));
-          y1 = fmaf(v[96], x0, fmaf(v[128], x1, fmaf(v[160], x2, y1)));
-          y2 = fmaf(v[192], x0, fmaf(v[224], x1, fmaf(v[256], x2, y2)));
-        }
-        float pq = 0.f;
-        if (row < A.voff[inst + 1]) {
-          float p[3];
+          float x[3];
 #pragma unroll
           for (int k = 0; k < 3; k++) {
-            p[k] = fmaf(beta, Pold[3 * row + k], A.z32[3 * row + k]);
-            Pnew[3 * row + k] = p[k];
+            const int i = 3 * col + k;
+            const float sk = first ? Wc[i] : fmaf(beta, Sp[i], Wc[i]);
+            x[k] = fmaf(-alpha, sk, Rc[i]);
           }
-          A.q32[3 * row + 0] = y0;
-          A.q32[3 * row + 1] = y1;
-          A.q32[3 * row + 2] = y2;
-          pq = p[0] * y0 + p[1] * y1 + p[2] * y2;
+          const float* v = V + 288 * j;
+          y0 = fmaf(v[0], x[0], fmaf(v[32], x[1], fmaf(v[64], x[2], y0)));
+          y1 = fmaf(v[96], x[0], fmaf(v[128], x[1], fmaf(v[160], x[2], y1)));
+          y2 = fmaf(v[192], x[0], fmaf(v[224], x[1], fmaf(v[256], x[2], y2)));
         }
-        pq = warp_sum_f(pq);
-        if (lane == 0) {
-          A.part32[3 * sl + 0] = pq;
-          if (A.count_bytes) {  // without the preconditioner no D^-1 is read (36 B a row)
-            const int rows = min(32, A.voff[inst + 1] - A.slice_row0[sl]);
-            atomicAdd(&A.bytes_acc[6], (unsigned long long)(A.slice_pbytes[sl] - (bjac ? 0 : 36LL * rows)));
-          }
-        }
-      }
-      if (last_portion(A, inst, hi - lo, &s_flag)) {
-        double tot[1];
-        cloth_totals<kPersistThreads>(A, inst, 0, 1, sh, tot);
-        if (threadIdx.x == 0) A.st[inst].alpha32 = (float)(A.st[inst].rzh[it & 1] / tot[0]);
-      }
-    }
-    if (!grid_sync(A)) return;
-    // ---- phase B: update, r.z and r.r, convergence or beta
-    for (int inst = R.c0; inst <= R.c1; inst++) {
-      int lo, hi;
-      if (!portion(A, R, compact, s_pref, inst, lo, hi)) continue;
-      InstState& St = A.st[inst];
-      const float alpha = St.alpha32;
-      const int bjac = St.bjac;
-      for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
-        const int row = A.slice_row0[sl] + lane;
-        float rz = 0.f, rr = 0.f;
+        float gam = 0.f, del = 0.f;
         if (row < A.voff[inst + 1]) {
-          float r[3], z[3];
+          const float y[3] = {y0, y1, y2};
 #pragma unroll
           for (int k = 0; k < 3; k++) {
             const int i = 3 * row + k;
-            A.d32[i] = fmaf(alpha, Pnew[i], A.d32[i]);
-            r[k] = fmaf(-alpha, A.q32[i], A.r32[i]);
-            A.r32[i] = r[k];
-          }
-          precondition(A, bjac, row, r, z);
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            A.z32[3 * row + k] = z[k];
-            rz += r[k] * z[k];
-            rr += r[k] * r[k];
+            const float sk = first ? Wc[i] : fmaf(beta, Sp[i], Wc[i]);
+            const float pk = first ? Rc[i] : fmaf(beta, A.p32[i], Rc[i]);
+            const float rn = fmaf(-alpha, sk, Rc[i]);
+            Sn[i] = sk;
+            A.p32[i] = pk;
+            A.d32[i] = fmaf(alpha, pk, A.d32[i]);
+            Rn[i] = rn;
+            Wn[i] = y[k];
+            gam += rn * rn;
+            del += y[k] * rn;
           }
         }
-        rz = warp_sum_f(rz);
-        rr = warp_sum_f(rr);
+        gam = warp_sum_f(gam);
+        del = warp_sum_f(del);
         if (lane == 0) {
-          A.part32[3 * sl + 1] = rz;
-          A.part32[3 * sl + 2] = rr;
+          A.part32[3 * sl + 0] = gam;
+          A.part32[3 * sl + 1] = del;
+          if (A.count_bytes) atomicAdd(&A.bytes_acc[6], (unsigned long long)A.slice_pbytes[sl]);
         }
       }
       if (last_portion(A, inst, hi - lo, &s_flag)) {
         double tot[2];
-        cloth_totals<kPersistThreads>(A, inst, 1, 2, sh, tot);
+        cloth_totals<kPersistThreads>(A, inst, 0, 2, sh, tot);
         if (threadIdx.x == 0) {
-          St.inner_iters = it;
-          if (tot[1] <= (double)eta * (double)eta * St.rr_in0 || it >= cap) {
-            St.istop = 1;
-            St.idone = 1;
-            St.red[1] = tot[0];
-            St.red[2] = tot[1];
+          InstState& Sw = A.st[inst];
+          Sw.inner_iters = it;
+          const double gam = tot[0], del = tot[1];
+          const double beta_n = gam / Sw.gam;
+          const double den = del - beta_n * gam / Sw.alf;
+          if (gam <= (double)eta * (double)eta * Sw.rr_in0 || it >= cap || !(den > 0.0)) {
+            Sw.istop = 1;
+            Sw.idone = 1;
+            Sw.red[2] = gam;
             atomicSub(&A.grid_bar[3], 1u);
           } else {
-            St.beta32 = (float)(tot[0] / St.rzh[it & 1]);
-            St.rzh[(it + 1) & 1] = tot[0];
+            Sw.alf = gam / den;
+            Sw.gam = gam;
+            Sw.alpha32 = (float)Sw.alf;
+            Sw.beta32 = (float)beta_n;
           }
         }
       }
@@ -547,17 +562,57 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads) k_mx_
   }
 }
 
-// inner-solve start for the persistent kernel: totals of r.z and r.r per cloth
-// and the count of cloths that iterate
+// start of the persistent inner solve: w_1 = A r_1 over the slices (r_1 = r32
+// from k_mx_inner_init), with the slice partials of gamma = r.r and delta = w.r
+__global__ void __launch_bounds__(kSliceThreads) k_mx_pw0(Arena A) {
+  SliceCtx c;
+  if (!slice_ctx(A, c, false)) return;
+  const int w = A.slice_w[c.slice];
+  const float* V = A.val32 + A.slice_voff[c.slice] + c.lane;
+  const int* Cc = A.col32 + A.slice_coff[c.slice] + c.lane;
+  float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+  for (int j = 0; j < w; j++) {
+    const int col = Cc[32 * j];
+    const float x0 = A.r32[3 * col + 0], x1 = A.r32[3 * col + 1], x2 = A.r32[3 * col + 2];
+    const float* v = V + 288 * j;
+    y0 = fmaf(v[0], x0, fmaf(v[32], x1, fmaf(v[64], x2, y0)));
+    y1 = fmaf(v[96], x0, fmaf(v[128], x1, fmaf(v[160], x2, y1)));
+    y2 = fmaf(v[192], x0, fmaf(v[224], x1, fmaf(v[256], x2, y2)));
+  }
+  float gam = 0.f, del = 0.f;
+  if (c.valid) {
+    const float y[3] = {y0, y1, y2};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float r = A.r32[3 * c.row + k];
+      A.w32[3 * c.row + k] = y[k];
+      gam += r * r;
+      del += y[k] * r;
+    }
+  }
+  gam = warp_sum_f(gam);
+  del = warp_sum_f(del);
+  if (c.lane == 0) {
+    A.part32[3 * c.slice + 0] = gam;
+    A.part32[3 * c.slice + 1] = del;
+    if (A.count_bytes) atomicAdd(&A.bytes_acc[0], (unsigned long long)A.slice_bytes[c.slice]);
+  }
+}
+
+// per-cloth totals of the start: gamma_1, alpha_1 = gamma_1 / delta_1, and the
+// count of cloths that iterate
 __global__ void k_mx_pstart(Arena A) {
   const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (inst >= A.ni || !A.active[inst] || A.st[inst].done) return;
-  const double rz = cloth_total(A, inst, 1), rr = cloth_total(A, inst, 2);
+  const double gam = cloth_total(A, inst, 0), del = cloth_total(A, inst, 1);
   if ((threadIdx.x & 31) == 0) {
     InstState& S = A.st[inst];
-    S.rzh[1] = rz;  // iteration 1 reads parity 1
-    S.rr_in0 = rr;
-    S.idone = (rr <= 0.0) ? 1 : 0;
+    S.rr_in0 = gam;
+    S.gam = gam;
+    S.alf = del > 0.0 ? gam / del : 0.0;
+    S.alpha32 = (float)S.alf;
+    S.beta32 = 0.f;
+    S.idone = (gam <= 0.0 || !(del > 0.0)) ? 1 : 0;
     S.istop = S.idone;
     S.inner_iters = 0;
     if (!S.idone) atomicAdd(&A.grid_bar[3], 1u);
@@ -637,13 +692,23 @@ __global__ void k_mx_warm(Arena A) {
   A.dx[i] = A.bc[i / 3] ? 0.0 : A.prm[inst].dt * A.v[i];
 }
 
-// dx += d (FP64)
+// dx += S^T d (scaled cloths) or d, in FP64
 __global__ void k_mx_correct(Arena A) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 3 * A.nv) return;
-  const int inst = A.vinst[i / 3];
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  const int inst = A.vinst[v];
   if (!A.active[inst] || A.st[inst].done) return;
-  A.dx[i] += (double)A.d32[i];
+  const double d0 = A.d32[3 * v], d1 = A.d32[3 * v + 1], d2 = A.d32[3 * v + 2];
+  if (A.st[inst].bjac) {
+    const float* S = A.linv32 + 9 * (size_t)v;
+    A.dx[3 * v + 0] += (double)S[0] * d0 + (double)S[3] * d1 + (double)S[6] * d2;
+    A.dx[3 * v + 1] += (double)S[4] * d1 + (double)S[7] * d2;
+    A.dx[3 * v + 2] += (double)S[8] * d2;
+  } else {
+    A.dx[3 * v + 0] += d0;
+    A.dx[3 * v + 1] += d1;
+    A.dx[3 * v + 2] += d2;
+  }
 }
 
 // r = b - A dx with the FP64 matrix; chunk partials of r.r
@@ -703,7 +768,8 @@ __global__ void k_mx_check(Arena A, double tol_in, int maxcycles) {
 void launch_mx_outer_init(const Arena& A, cudaStream_t s) {
   k_mx_outer_init<<<A.nchunk, kChunk, 0, s>>>(A);
   k_mx_outer_start<<<(A.ni + 127) / 128, 128, 0, s>>>(A);
-  g_launches += 2;
+  k_mx_scale<<<(A.nslice * 32 + kSliceThreads - 1) / kSliceThreads, kSliceThreads, 0, s>>>(A);
+  g_launches += 3;
 }
 
 void launch_mx_warm_start(const Arena& A, cudaStream_t s) {
@@ -759,8 +825,9 @@ void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_p
   launch_check(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(A.ni, 1), s), "cudaMemsetAsync");
   const int blocks = (A.nslice * 32 + kSliceThreads - 1) / kSliceThreads;
   k_mx_inner_init<<<blocks, kSliceThreads, 0, s>>>(A);
+  k_mx_pw0<<<blocks, kSliceThreads, 0, s>>>(A);
   k_mx_pstart<<<(A.ni * 32 + 127) / 128, 128, 0, s>>>(A);
-  g_launches += 2;
+  g_launches += 3;
   if (threads == 1024)
     persist_launch<1024>(A, eta, cap, blocks_per_sm, s);
   else if (threads == 512)
@@ -770,7 +837,7 @@ void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_p
 }
 
 void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s) {
-  k_mx_correct<<<(3 * A.nv + 255) / 256, 256, 0, s>>>(A);
+  k_mx_correct<<<(A.nv + 255) / 256, 256, 0, s>>>(A);
   prof_begin(PK_MX_RESIDUAL, s);
   k_mx_residual<<<A.nchunk, kChunk, 0, s>>>(A);
   prof_end(PK_MX_RESIDUAL, s);

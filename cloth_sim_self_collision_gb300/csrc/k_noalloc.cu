@@ -15,6 +15,8 @@
 // * the array's device address is looked up once per device, on the first
 //   call made with that device current; make that first call before any stream
 //   capture;
+// * every call copies the convergence ratio and iteration count to the host
+//   and waits for its stream before returning;
 // * every call shares the one array, so calls that overlap on the GPU (on
 //   different streams or devices' contexts racing on the same device) corrupt
 //   each other: serialise them;

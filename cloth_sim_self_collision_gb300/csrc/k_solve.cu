@@ -451,6 +451,33 @@ __global__ void k_spmv_all(Arena A, const double* x, double* y) {
   spmv_row(A, i, x, y);
 }
 
+// y = beta y + alpha A x over rows [v0, v1), in the operation order of
+// MatVec's 3x3 branch (matrix_square_sparse.cpp:218-242)
+__global__ void k_matvec_rows(Arena A, int v0, int v1, double alpha, const double* x, double beta, double* y) {
+  const int i = v0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v1) return;
+  double y0 = y[3 * i + 0] * beta, y1 = y[3 * i + 1] * beta, y2 = y[3 * i + 2] * beta;
+  for (int s = A.row_ptr[i]; s < A.row_ptr[i + 1]; s++) {
+    const int j = A.col_idx[s];
+    const double* a = A.vcrs + 9 * (size_t)s;
+    const double x0 = x[3 * j + 0], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+    y0 += alpha * (a[0] * x0 + a[1] * x1 + a[2] * x2);
+    y1 += alpha * (a[3] * x0 + a[4] * x1 + a[5] * x2);
+    y2 += alpha * (a[6] * x0 + a[7] * x1 + a[8] * x2);
+  }
+  const double* a = A.vdia + 9 * (size_t)i;
+  const double x0 = x[3 * i + 0], x1 = x[3 * i + 1], x2 = x[3 * i + 2];
+  y0 += alpha * (a[0] * x0 + a[1] * x1 + a[2] * x2);
+  y1 += alpha * (a[3] * x0 + a[4] * x1 + a[5] * x2);
+  y2 += alpha * (a[6] * x0 + a[7] * x1 + a[8] * x2);
+  y[3 * i + 0] = y0;
+  y[3 * i + 1] = y1;
+  y[3 * i + 2] = y2;
+}
+
+// CPreconditionerILU::Solve (ilu_sparse.h:23-26): z <- (LU)^-1 z for one cloth
+__global__ void __launch_bounds__(kSolveThreads) k_ilu_solve(Arena A, int inst, double* z) { ilu_apply(A, inst, z); }
+
 }  // namespace
 
 void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s) {
@@ -498,6 +525,18 @@ void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, bool ser
 
 void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s) {
   k_spmv_all<<<(A.nv + 127) / 128, 128, 0, s>>>(A, x, y);
+  g_launches++;
+}
+
+void launch_matvec(const Arena& A, int v0, int v1, double alpha, const double* x, double beta, double* y,
+                   cudaStream_t s) {
+  if (v1 <= v0) return;
+  k_matvec_rows<<<(v1 - v0 + 127) / 128, 128, 0, s>>>(A, v0, v1, alpha, x, beta, y);
+  g_launches++;
+}
+
+void launch_ilu_solve(const Arena& A, int inst, double* z, cudaStream_t s) {
+  k_ilu_solve<<<1, kSolveThreads, 0, s>>>(A, inst, z);
   g_launches++;
 }
 

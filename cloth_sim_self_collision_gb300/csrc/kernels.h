@@ -59,6 +59,11 @@ void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, c
 void launch_cg_init(const Arena& A, double tol, int maxit, cudaStream_t s);
 void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, bool serial, cudaStream_t s);
 void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s);
+// y = beta y + alpha A x over the rows [v0, v1) (MatVec's operation order)
+void launch_matvec(const Arena& A, int v0, int v1, double alpha, const double* x, double beta, double* y,
+                   cudaStream_t s);
+// (LU)^-1 z in place with the last ILU(0) factor of cloth slot inst
+void launch_ilu_solve(const Arena& A, int inst, double* z, cudaStream_t s);
 
 // --- mixed precision (k_mixed.cu) ----------------------------------------------
 void launch_mx_outer_init(const Arena& A, cudaStream_t s);
@@ -99,6 +104,11 @@ void launch_riz_add(const Arena& A, const ContactBufs& C, int nce, cudaStream_t 
 // zone rigid velocities: v of zone members from snapshot v0 at positions xs
 void riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, const double* v0s, cudaStream_t s);
 int riz_count_zones(const Arena& A, ContactBufs& C, int* zone_of_vertex_dev, cudaStream_t s);
+
+// geometry on batches (bvh_aabb.cpp:321-384, 598-662), 12 doubles of points per item
+void launch_distance_fv(int n, const double* pts, double* dist, double* w, cudaStream_t s);
+void launch_distance_ee(int n, const double* pts, double* dist, double* ratio, cudaStream_t s);
+void launch_coplanar_time(int n, const double* s0, const double* e0, double* t, cudaStream_t s);
 
 size_t cub_sort_bytes(int n);
 void cub_sort_pairs(void* tmp, size_t bytes, const unsigned long long* kin, unsigned long long* kout,

@@ -71,6 +71,49 @@ bool CMatrixSquareSparse::SetZero() {
   return true;
 }
 
+// Mearge (matrix_square_sparse.cpp:88-138): adds an element matrix into the
+// caller's host container, diagonal blocks to m_valDia and the pattern's
+// off-diagonal blocks to m_valCrs (blocks outside the pattern are dropped)
+bool CMatrixSquareSparse::Mearge(int nblkel_col, const int* blkel_col, int nblkel_row, const int* blkel_row,
+                                 int blksize, const double* emat, std::vector<int>& buf) {
+  assert(nblkel_col == nblkel_row && blksize == m_len * m_len);
+  if ((int)buf.size() < m_nblk) buf.assign(m_nblk, -1);
+  for (int a = 0; a < nblkel_col; a++) {
+    const int row = blkel_col[a];
+    for (int k = m_colInd[row]; k < m_colInd[row + 1]; k++) buf[m_rowPtr[k]] = k;
+    for (int b = 0; b < nblkel_row; b++) {
+      const double* in = emat + (size_t)(a * nblkel_row + b) * blksize;
+      double* out;
+      if (a == b) {
+        out = m_valDia + (size_t)row * blksize;
+      } else {
+        const int slot = buf[blkel_row[b]];
+        if (slot < 0) continue;
+        out = m_valCrs + (size_t)slot * blksize;
+      }
+      for (int e = 0; e < blksize; e++) out[e] += in[e];
+    }
+    for (int k = m_colInd[row]; k < m_colInd[row + 1]; k++) buf[m_rowPtr[k]] = -1;
+  }
+  return true;
+}
+
+// SetBoundaryCondition (matrix_square_sparse.cpp:272-302): identity diagonal
+// and zero off-diagonal blocks in the rows and columns of fixed vertices
+void CMatrixSquareSparse::SetBoundaryCondition(const std::vector<int>& bc_flag) {
+  const size_t bs = (size_t)m_len * m_len;
+  for (int i = 0; i < m_nblk; i++) {
+    if (bc_flag[i] == 0) continue;
+    for (size_t e = 0; e < bs; e++) m_valDia[i * bs + e] = 0.0;
+    for (int d = 0; d < m_len; d++) m_valDia[i * bs + (size_t)d * m_len + d] = 1.0;
+    for (int k = m_colInd[i]; k < m_colInd[i + 1]; k++)
+      for (size_t e = 0; e < bs; e++) m_valCrs[k * bs + e] = 0.0;
+  }
+  for (int k = 0; k < m_ncrs; k++)
+    if (bc_flag[m_rowPtr[k]] != 0)
+      for (size_t e = 0; e < bs; e++) m_valCrs[k * bs + e] = 0.0;
+}
+
 CPreconditionerILU::CPreconditionerILU() : m_diaInd(nullptr) {}
 CPreconditionerILU::~CPreconditionerILU() { delete[] m_diaInd; }
 
@@ -193,6 +236,8 @@ struct State {
   std::map<PdFn, Obstacle> obstacles;
   std::map<ClothKey, int> cloths;
   std::map<const int*, int> by_tri;
+  std::map<const CMatrixSquareSparse*, int> by_matrix;
+  std::map<int, int> nverts;  // cloth id -> vertices
   std::map<int, cs_params> params;
   double ilu_tol = 1.0e-4, cg_tol = 1.0e-4;
   int ilu_maxit = 100, cg_maxit = 1000;
@@ -247,6 +292,7 @@ bool cloth_for(const std::vector<double>& X0, const std::vector<int>& bc, const 
   s.cloths[key] = *id;
   s.by_tri[tri.data()] = *id;
   s.params[*id] = prm;
+  s.nverts[*id] = np;
   return true;
 }
 
@@ -299,9 +345,76 @@ void implicit_step(std::vector<double>& aXYZ, std::vector<double>& aUVW, CMatrix
   aXYZ.swap(x);
   aUVW.swap(v);
   // the assembled matrix and its factor stay on the device; mat_A / ilu_A keep
-  // the caller's pattern (the reference's driver never reads their values)
-  (void)mat_A;
-  (void)ilu_A;
+  // the caller's pattern (the reference's driver never reads their values) and
+  // name the cloth for the matrix functions
+  s.by_matrix[&mat_A] = id;
+  if (ilu_A) s.by_matrix[&ilu_A->mat] = id;
+}
+
+// the cloth whose matrix pattern m carries: the one it was passed with to a
+// StepTime function, else an admitted cloth with the same pattern
+bool cloth_of_matrix(const CMatrixSquareSparse& m, int* id) {
+  State& s = S();
+  auto it = s.by_matrix.find(&m);
+  if (it != s.by_matrix.end()) {
+    *id = it->second;
+    return true;
+  }
+  if (m.m_len != 3) return fail(CS_ERR_ARG, "only 3x3 block matrices run on the device");
+  for (const auto& kv : s.nverts) {
+    int nb = 0;
+    if (kv.second != m.m_nblk || cs_pattern(s.ctx, kv.first, &nb, nullptr, nullptr) != CS_OK || nb != m.m_ncrs)
+      continue;
+    std::vector<int> rp((size_t)m.m_nblk + 1), ci((size_t)std::max(nb, 1));
+    if (cs_pattern(s.ctx, kv.first, nullptr, rp.data(), ci.data()) != CS_OK) continue;
+    if (std::equal(rp.begin(), rp.end(), m.m_colInd) && std::equal(ci.begin(), ci.begin() + nb, m.m_rowPtr)) {
+      s.by_matrix[&m] = kv.first;
+      *id = kv.first;
+      return true;
+    }
+  }
+  return fail(CS_ERR_ARG, "matrix pattern belongs to no admitted cloth (pass it to a StepTime function first)");
+}
+
+// uploads the values of m as the cloth's device matrix
+bool upload_matrix(const CMatrixSquareSparse& m, int* id) {
+  State& s = S();
+  if (!ensure_ctx() || !cloth_of_matrix(m, id)) return false;
+  const int rc = cs_set_matrix(s.ctx, *id, m.m_valDia, m.m_valCrs);
+  if (rc != CS_OK) return fail(rc, cs_last_error(s.ctx));
+  return true;
+}
+
+// the cloth of aTri for the BVH functions (admitted with aXYZ as its rest
+// shape, no stencils, when it is new)
+bool cloth_of_mesh(const std::vector<int>& aTri, const std::vector<double>& aXYZ, int* id) {
+  State& s = S();
+  if (!ensure_ctx()) return false;
+  auto it = s.by_tri.find(aTri.data());
+  if (it != s.by_tri.end()) {
+    *id = it->second;
+    return true;
+  }
+  const double g[3] = {0, 0, 0};
+  cs_params p = make_params(0.0, 0, 0, 0, g, 1.0, 0.0, 0.0, CS_SOLVER_CG);
+  std::vector<int> bc, quad;
+  return cloth_for(aXYZ, bc, aTri, quad, p, id);
+}
+
+void boxes_to(const std::vector<double>& boxes, int nnode, int ibvh, const std::vector<CNodeBVH>& nodes,
+              std::vector<CAABB3D>& aBB) {
+  aBB.resize(std::max<size_t>(nodes.size(), (size_t)nnode));
+  for (int n = 0; n < nnode; n++) {
+    CAABB3D& b = aBB[n];
+    b.x_min = boxes[7 * n + 0];
+    b.x_max = boxes[7 * n + 1];
+    b.y_min = boxes[7 * n + 2];
+    b.y_max = boxes[7 * n + 3];
+    b.z_min = boxes[7 * n + 4];
+    b.z_max = boxes[7 * n + 5];
+    b.isnt_empty = boxes[7 * n + 6] != 0.0;
+  }
+  (void)ibvh;
 }
 
 }  // namespace
@@ -414,17 +527,7 @@ void GetIntermidiateVelocityContactResolved(std::vector<double>& aUVWm, bool& is
     fail(rc, cs_last_error(s.ctx));
     return;
   }
-  aBB.resize(std::max<size_t>(aNodeBVH.size(), (size_t)nnode));
-  for (int n = 0; n < nnode; n++) {
-    CAABB3D& b = aBB[n];
-    b.x_min = boxes[7 * n + 0];
-    b.x_max = boxes[7 * n + 1];
-    b.y_min = boxes[7 * n + 2];
-    b.y_max = boxes[7 * n + 3];
-    b.z_min = boxes[7 * n + 4];
-    b.z_max = boxes[7 * n + 5];
-    b.isnt_empty = boxes[7 * n + 6] != 0.0;
-  }
+  boxes_to(boxes, nnode, 0, aNodeBVH, aBB);
 }
 
 int MakeBVHTopology_TopDown(const std::vector<int>& aTri, const std::vector<double>& aXYZ,
@@ -445,6 +548,256 @@ int MakeBVHTopology_TopDown(const std::vector<int>& aTri, const std::vector<doub
     aNodeBVH[n].ichild[1] = nodes[3 * n + 2];
   }
   return 0;
+}
+
+// ---- lower-level functions on the device ------------------------------------------
+
+void CMatrixSquareSparse::MatVec(double alpha, const std::vector<double>& x, double beta,
+                                 std::vector<double>& y) const {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (!upload_matrix(*this, &id)) return;
+  const int rc = cs_matvec(s.ctx, id, alpha, x.data(), beta, y.data());
+  if (rc != CS_OK) fail(rc, cs_last_error(s.ctx));
+}
+
+void Solve_CG(double& conv_ratio, int& iteration, const CMatrixSquareSparse& mat, std::vector<double>& r_vec,
+              std::vector<double>& u_vec) {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (!upload_matrix(mat, &id)) return;
+  u_vec.resize(r_vec.size());
+  double conv = 0.0;
+  int iter = 0;
+  int rc = cs_solve_cg(s.ctx, id, r_vec.data(), conv_ratio, iteration, u_vec.data(), &conv, &iter);
+  if (rc == CS_OK) rc = cs_last_residual(s.ctx, id, r_vec.data());
+  if (rc != CS_OK) {
+    fail(rc, cs_last_error(s.ctx));
+    return;
+  }
+  conv_ratio = conv;
+  iteration = iter;
+}
+
+void CPreconditionerILU::DoILUDecomp() {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (!upload_matrix(mat, &id)) return;
+  int nsing = 0;
+  const int rc = cs_ilu_factor(s.ctx, id, mat.m_valDia, mat.m_valCrs, &nsing);
+  if (rc != CS_OK) fail(rc, cs_last_error(s.ctx));
+}
+
+void CPreconditionerILU::Solve(std::vector<double>& vec) const {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (!ensure_ctx() || !cloth_of_matrix(mat, &id)) return;
+  const int rc = cs_ilu_solve(s.ctx, id, vec.data());
+  if (rc != CS_OK) fail(rc, cs_last_error(s.ctx));
+}
+
+void Solve_PCG(double& conv_ratio, int& iteration, const CMatrixSquareSparse& mat, const CPreconditionerILU& ilu,
+               std::vector<double>& r_vec, std::vector<double>& u_vec) {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id, idf;
+  if (!upload_matrix(mat, &id) || !cloth_of_matrix(ilu.mat, &idf)) return;
+  if (id != idf) {
+    fail(CS_ERR_ARG, "Solve_PCG: the matrix and the preconditioner belong to different cloths");
+    return;
+  }
+  u_vec.resize(r_vec.size());
+  double conv = 0.0;
+  int iter = 0;
+  int rc = cs_solve_pcg(s.ctx, id, r_vec.data(), conv_ratio, iteration, u_vec.data(), &conv, &iter);
+  if (rc == CS_OK) rc = cs_last_residual(s.ctx, id, r_vec.data());
+  if (rc != CS_OK) {
+    fail(rc, cs_last_error(s.ctx));
+    return;
+  }
+  conv_ratio = conv;
+  iteration = iter;
+}
+
+void BuildBoundingBoxChild_Prx(int ibvh, double delta, const std::vector<double>& aXYZ, const std::vector<int>& aTri,
+                               const std::vector<CNodeBVH>& aNodeBVH, std::vector<CAABB3D>& aBB) {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (ibvh != 0) {
+    fail(CS_ERR_ARG, "BuildBoundingBoxChild_Prx: only the root node (0) is refitted on the device");
+    return;
+  }
+  if (!cloth_of_mesh(aTri, aXYZ, &id)) return;
+  int nnode = 0;
+  cs_bvh_nodes(s.ctx, id, &nnode, nullptr);
+  std::vector<double> boxes(7 * (size_t)nnode);
+  const int rc = cs_refit_prx(s.ctx, id, aXYZ.data(), delta, boxes.data());
+  if (rc != CS_OK) {
+    fail(rc, cs_last_error(s.ctx));
+    return;
+  }
+  boxes_to(boxes, nnode, ibvh, aNodeBVH, aBB);
+}
+
+void BuildBoundingBoxChild_CCD(int ibvh, double dt, const std::vector<double>& aXYZ, const std::vector<double>& aUVW,
+                               const std::vector<int>& aTri, const std::vector<CNodeBVH>& aNodeBVH,
+                               std::vector<CAABB3D>& aBB) {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (ibvh != 0) {
+    fail(CS_ERR_ARG, "BuildBoundingBoxChild_CCD: only the root node (0) is refitted on the device");
+    return;
+  }
+  if (!cloth_of_mesh(aTri, aXYZ, &id)) return;
+  int nnode = 0;
+  cs_bvh_nodes(s.ctx, id, &nnode, nullptr);
+  std::vector<double> boxes(7 * (size_t)nnode);
+  const int rc = cs_refit_ccd(s.ctx, id, aXYZ.data(), aUVW.data(), dt, boxes.data());
+  if (rc != CS_OK) {
+    fail(rc, cs_last_error(s.ctx));
+    return;
+  }
+  boxes_to(boxes, nnode, ibvh, aNodeBVH, aBB);
+}
+
+namespace {
+// contacts of one detection into a std::set (the reference's container)
+template <typename F>
+void contacts_into(std::set<CContactElement>& out, F&& detect) {
+  State& s = S();
+  int n = 0;
+  std::vector<int> buf(5 * 4096);
+  int rc = detect(buf.data(), 4096, &n);
+  if (rc == CS_ERR_CAPACITY && n > 4096) {
+    buf.assign(5 * (size_t)n, 0);
+    rc = detect(buf.data(), n, &n);
+  }
+  if (rc != CS_OK) {
+    fail(rc, cs_last_error(s.ctx));
+    return;
+  }
+  for (int e = 0; e < n; e++) {
+    const int* c = buf.data() + 5 * (size_t)e;
+    // the stored key is canonical already: the constructor keeps it
+    out.insert(CContactElement(c[0] != 0, c[1], c[2], c[3], c[4]));
+  }
+}
+}  // namespace
+
+void GetContactElement_Proximity(std::set<CContactElement>& aContactElem, double delta,
+                                 const std::vector<double>& aXYZ, const std::vector<int>& aTri, int ibvh,
+                                 const std::vector<CNodeBVH>& aBVH, const std::vector<CAABB3D>& aBB) {
+  (void)aBVH;
+  (void)aBB;
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (ibvh != 0) {
+    fail(CS_ERR_ARG, "GetContactElement_Proximity: only the root node (0) is searched on the device");
+    return;
+  }
+  if (!cloth_of_mesh(aTri, aXYZ, &id)) return;
+  contacts_into(aContactElem, [&](int* out, int cap, int* n) {
+    return cs_contacts_prx(s.ctx, id, aXYZ.data(), delta, out, cap, n);
+  });
+}
+
+void GetContactElement_CCD(std::set<CContactElement>& aContactElem, double dt, double delta,
+                           const std::vector<double>& aXYZ, const std::vector<double>& aUVW,
+                           const std::vector<int>& aTri, int ibvh, const std::vector<CNodeBVH>& aBVH,
+                           const std::vector<CAABB3D>& aBB) {
+  (void)aBVH;
+  (void)aBB;
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  int id;
+  if (ibvh != 0) {
+    fail(CS_ERR_ARG, "GetContactElement_CCD: only the root node (0) is searched on the device");
+    return;
+  }
+  if (!cloth_of_mesh(aTri, aXYZ, &id)) return;
+  contacts_into(aContactElem, [&](int* out, int cap, int* n) {
+    return cs_contacts_ccd(s.ctx, id, aXYZ.data(), aUVW.data(), dt, delta, out, cap, n);
+  });
+}
+
+namespace {
+void put(double* d, const CVector3D& v) {
+  d[0] = v.x;
+  d[1] = v.y;
+  d[2] = v.z;
+}
+}  // namespace
+
+double DistanceFaceVertex(const CVector3D& p0, const CVector3D& p1, const CVector3D& p2, const CVector3D& p3,
+                          double& w0, double& w1) {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  double pts[12], dist = 0.0, w[2] = {0.0, 0.0};
+  put(pts, p0);
+  put(pts + 3, p1);
+  put(pts + 6, p2);
+  put(pts + 9, p3);
+  if (!ensure_ctx()) return 0.0;
+  const int rc = cs_distance_fv(s.ctx, 1, pts, &dist, w);
+  if (rc != CS_OK) fail(rc, cs_last_error(s.ctx));
+  w0 = w[0];
+  w1 = w[1];
+  return dist;
+}
+
+double DistanceEdgeEdge(const CVector3D& p0, const CVector3D& p1, const CVector3D& q0, const CVector3D& q1,
+                        double& ratio_p, double& ratio_q) {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  double pts[12], dist = 0.0, r[2] = {0.0, 0.0};
+  put(pts, p0);
+  put(pts + 3, p1);
+  put(pts + 6, q0);
+  put(pts + 9, q1);
+  if (!ensure_ctx()) return 0.0;
+  const int rc = cs_distance_ee(s.ctx, 1, pts, &dist, r);
+  if (rc != CS_OK) fail(rc, cs_last_error(s.ctx));
+  ratio_p = r[0];
+  ratio_q = r[1];
+  return dist;
+}
+
+double FindCoplanerInterp(const CVector3D& s0, const CVector3D& s1, const CVector3D& s2, const CVector3D& s3,
+                          const CVector3D& e0, const CVector3D& e1, const CVector3D& e2, const CVector3D& e3) {
+  State& s = S();
+  std::lock_guard<std::mutex> lock(s.mu);
+  s.status = CS_OK;
+  double a[12], b[12], t = -1.0;
+  put(a, s0);
+  put(a + 3, s1);
+  put(a + 6, s2);
+  put(a + 9, s3);
+  put(b, e0);
+  put(b + 3, e1);
+  put(b + 6, e2);
+  put(b + 9, e3);
+  if (!ensure_ctx()) return -1.0;
+  const int rc = cs_coplanar_time(s.ctx, 1, a, b, &t);
+  if (rc != CS_OK) fail(rc, cs_last_error(s.ctx));
+  return t;
 }
 
 void ClothGpuRegisterObstacle(void (*penetrationDepth)(double&, double*, const double*), int kind,

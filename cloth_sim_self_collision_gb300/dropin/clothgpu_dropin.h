@@ -9,10 +9,17 @@
 //   UpdateIntermidiateVelocity        solve_internal_sparse.h:329-343
 //   GetIntermidiateVelocityContactResolved  self_collision_cloth.h:21-34
 //   MakeBVHTopology_TopDown           bvh_aabb.h:25-28
-//   CMatrixSquareSparse (Initialize, SetPattern, SetZero)   matrix_square_sparse.h:14-48
-//   CPreconditionerILU (Initialize_ILU0, SetValueILU)      ilu_sparse.h:16-34
+//   BuildBoundingBoxChild_Prx / _CCD  bvh_aabb.h:31-46
+//   GetContactElement_Proximity / _CCD                      bvh_aabb.h:110-130
+//   DistanceFaceVertex, DistanceEdgeEdge, FindCoplanerInterp bvh_aabb.h:49-61
+//   CMatrixSquareSparse (Initialize, SetPattern, SetZero, Mearge, MatVec,
+//                        SetBoundaryCondition)              matrix_square_sparse.h:14-48
+//   Solve_CG                          matrix_square_sparse.h:58-63
+//   CPreconditionerILU (Initialize_ILU0, SetValueILU, DoILUDecomp, Solve)  ilu_sparse.h:16-34
+//   Solve_PCG                         ilu_sparse.h:37-43
 //   CJaggedArray (SetNodeToElem, SetEdgeOfElem, Sort)       jagged_array.h:20-264
-//   CNodeBVH, CAABB3D, CContactElement                      bvh_aabb.h:18-106, aabb.h:16-148
+//   CNodeBVH, CAABB3D, CContactElement, CVector3D           bvh_aabb.h:18-106, aabb.h:16-148,
+//                                                           vector3d.h
 //
 // The frame functions forward to the C ABI (include/clothgpu.h): a cloth is
 // identified by its triangle and stencil arrays, admitted on first use with
@@ -20,6 +27,18 @@
 // reference's penetration-depth callback cannot run on a device: register it
 // once with ClothGpuRegisterObstacle (an unregistered callback makes the call
 // fail, reported by ClothGpuLastStatus, with the state left unchanged).
+//
+// The lower-level functions run on the device too.  The BVH functions take
+// the cloth of aTri (admitted with aXYZ as its rest shape if it is new) and
+// recompute the boxes from aXYZ as the matching BuildBoundingBoxChild_* call
+// would; they accept the root node only.  The containers stay on the host, as
+// in the reference: Mearge, SetZero and SetBoundaryCondition edit the caller's
+// arrays, and MatVec, Solve_CG, DoILUDecomp, ILU Solve and Solve_PCG upload
+// the matrix values to the cloth whose pattern the matrix carries (the matrix
+// passed to a StepTime function, or any matrix with an admitted cloth's
+// pattern) and compute there.  DoILUDecomp writes the factor back into the
+// preconditioner's matrix; Solve uses the factor of that cloth's last
+// DoILUDecomp or implicit step.
 //
 // Defaults reproduce the reference: FP64 with serial inner products (bit-exact
 // frames), PCG tolerance 1e-4 / 100 iterations and CG 1e-4 / 1000 as hard-coded
@@ -34,6 +53,15 @@
 
 // ---- containers (host side, the reference's data layout) -------------------------
 
+class CVector3D {
+ public:
+  CVector3D() : x(0), y(0), z(0) {}
+  CVector3D(double vx, double vy, double vz) : x(vx), y(vy), z(vz) {}
+
+ public:
+  double x, y, z;
+};
+
 class CMatrixSquareSparse {
  public:
   CMatrixSquareSparse();
@@ -43,6 +71,11 @@ class CMatrixSquareSparse {
   void operator=(const CMatrixSquareSparse& m);
   void SetPattern(const std::vector<int>& colind, const std::vector<int>& rowptr);
   bool SetZero();
+  bool Mearge(int nblkel_col, const int* blkel_col, int nblkel_row, const int* blkel_row, int blksize,
+              const double* emat, std::vector<int>& m_marge_tmp_buffer);
+  // {y} = alpha * [A]{x} + beta * {y}
+  void MatVec(double alpha, const std::vector<double>& x, double beta, std::vector<double>& y) const;
+  void SetBoundaryCondition(const std::vector<int>& bc_flag);
 
  public:
   int m_nblk;
@@ -63,11 +96,19 @@ class CPreconditionerILU {
   ~CPreconditionerILU();
   void Initialize_ILU0(const CMatrixSquareSparse& m);
   void SetValueILU(const CMatrixSquareSparse& m);
+  void Solve(std::vector<double>& vec) const;
+  void DoILUDecomp();
 
  public:
   CMatrixSquareSparse mat;
   int* m_diaInd;
 };
+
+void Solve_CG(double& conv_ratio, int& iteration, const CMatrixSquareSparse& mat, std::vector<double>& r_vec,
+              std::vector<double>& u_vec);
+
+void Solve_PCG(double& conv_ratio, int& iteration, const CMatrixSquareSparse& mat, const CPreconditionerILU& ilu,
+               std::vector<double>& r_vec, std::vector<double>& u_vec);
 
 class CJaggedArray {
  public:
@@ -148,6 +189,31 @@ void GetIntermidiateVelocityContactResolved(std::vector<double>& aUVWm, bool& is
 
 int MakeBVHTopology_TopDown(const std::vector<int>& aTri, const std::vector<double>& aXYZ,
                             std::vector<CNodeBVH>& aNodeBVH);
+
+void BuildBoundingBoxChild_Prx(int ibvh, double delta, const std::vector<double>& aXYZ, const std::vector<int>& aTri,
+                               const std::vector<CNodeBVH>& aNodeBVH, std::vector<CAABB3D>& aBB);
+
+void BuildBoundingBoxChild_CCD(int ibvh, double dt, const std::vector<double>& aXYZ, const std::vector<double>& aUVW,
+                               const std::vector<int>& aTri, const std::vector<CNodeBVH>& aNodeBVH,
+                               std::vector<CAABB3D>& aBB);
+
+double DistanceFaceVertex(const CVector3D& p0, const CVector3D& p1, const CVector3D& p2, const CVector3D& p3,
+                          double& w0, double& w1);
+
+double DistanceEdgeEdge(const CVector3D& p0, const CVector3D& p1, const CVector3D& q0, const CVector3D& q1,
+                        double& ratio_p, double& ratio_q);
+
+double FindCoplanerInterp(const CVector3D& s0, const CVector3D& s1, const CVector3D& s2, const CVector3D& s3,
+                          const CVector3D& e0, const CVector3D& e1, const CVector3D& e2, const CVector3D& e3);
+
+void GetContactElement_Proximity(std::set<CContactElement>& aContactElem, double delta,
+                                 const std::vector<double>& aXYZ, const std::vector<int>& aTri, int ibvh,
+                                 const std::vector<CNodeBVH>& aBVH, const std::vector<CAABB3D>& aBB);
+
+void GetContactElement_CCD(std::set<CContactElement>& aContactElem, double dt, double delta,
+                           const std::vector<double>& aXYZ, const std::vector<double>& aUVW,
+                           const std::vector<int>& aTri, int ibvh, const std::vector<CNodeBVH>& aBVH,
+                           const std::vector<CAABB3D>& aBB);
 
 // ---- extensions ------------------------------------------------------------------
 

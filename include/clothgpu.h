@@ -36,7 +36,8 @@ extern "C" {
 
 /* precision of the implicit solve */
 #define CS_PREC_FP64 0        /* plain: FP64 throughout, bit-exact with the reference */
-#define CS_PREC_MIXED 1       /* FP32 element/SpMV/CG + FP64 iterative refinement     */
+#define CS_PREC_MIXED 1       /* FP64 elements and assembly; FP32 SpMV/CG inside FP64
+                                 iterative refinement; collision in FP64               */
 
 /* obstacle kinds (replace the penetrationDepth callback,
  * self_contact_sparse/main.cpp:110-133) */
@@ -162,8 +163,25 @@ int cs_solve_pcg(cs_ctx *ctx, int id, const double *b, double tol, int maxit, do
 /* Solve_CG (matrix_square_sparse.cpp:338-406) on the last assembled matrix. */
 int cs_solve_cg(cs_ctx *ctx, int id, const double *b, double tol, int maxit, double *x, double *conv,
                 int *iter);
+/* The residual vector of the cloth's last cs_solve_cg / cs_solve_pcg: the r_vec
+ * that Solve_CG / Solve_PCG leave behind (matrix_square_sparse.cpp:338-406,
+ * ilu_sparse.cpp:628-709). */
+int cs_last_residual(cs_ctx *ctx, int id, double *r);
 /* CMatrixSquareSparse::MatVec(1, x, 0, y) (matrix_square_sparse.cpp:167-270) */
 int cs_spmv(cs_ctx *ctx, int id, const double *x, double *y);
+/* CMatrixSquareSparse::MatVec(alpha, x, beta, y) (matrix_square_sparse.cpp:167-270):
+ * y = beta y + alpha A x, y in place, in the reference's operation order. */
+int cs_matvec(cs_ctx *ctx, int id, double alpha, const double *x, double beta, double *y);
+/* Replaces the cloth's device matrix by caller values (diagonal blocks vdia[9 np],
+ * off-diagonal vcrs[9 nb] in the pattern's order; either may be null to keep it):
+ * the matrix a CMatrixSquareSparse holds after Mearge / SetBoundaryCondition
+ * (matrix_square_sparse.cpp:88-138, 272-302), for the MatVec, Solve_CG,
+ * DoILUDecomp and Solve_PCG entries above.  The next frame assembles anew. */
+int cs_set_matrix(cs_ctx *ctx, int id, const double *vdia, const double *vcrs);
+/* CPreconditionerILU::Solve (ilu_sparse.h:23-26: ForwardSubstitution then
+ * BackwardSubstitution, ilu_sparse.cpp:136-350): vec <- (LU)^-1 vec in place
+ * with the cloth's last factor (cs_ilu_factor). */
+int cs_ilu_solve(cs_ctx *ctx, int id, double *vec);
 
 /* BVH of a cloth: nnode and, when non-null, nodes[3 nnode] = parent, child0,
  * child1 (CNodeBVH, bvh_aabb.h:18-23; child1 == -1 marks a leaf). */
@@ -205,6 +223,17 @@ int cs_element_bend(cs_ctx *ctx, int n, const double *C, const double *c, double
 /* WdWddW_Contact (:243-280) for n points against the obstacle of prm */
 int cs_element_contact(cs_ctx *ctx, int n, const double *c, const cs_params *prm, double *W, double *dW,
                        double *ddW);
+
+/* ---- geometry on batches (bvh_aabb.h:50-61), on the device ---------------------- */
+/* DistanceFaceVertex (bvh_aabb.cpp:321-340) for n items: pts[n][12] = face p0 p1 p2
+ * and vertex p3; dist[n], w[n][2] = the weights of p0 and p1. */
+int cs_distance_fv(cs_ctx *ctx, int n, const double *pts, double *dist, double *w);
+/* DistanceEdgeEdge (bvh_aabb.cpp:343-384): pts[n][12] = p0 p1 q0 q1; dist[n],
+ * ratio[n][2] = ratio_p, ratio_q. */
+int cs_distance_ee(cs_ctx *ctx, int n, const double *pts, double *dist, double *ratio);
+/* FindCoplanerInterp (bvh_aabb.cpp:598-662): start points s[n][12], end points
+ * e[n][12]; t[n] = first coplanarity time in [0, 1], or -1. */
+int cs_coplanar_time(cs_ctx *ctx, int n, const double *s, const double *e, double *t);
 
 /* ---- whole-arena state I/O ------------------------------------------------------ */
 /* States of every cloth in the order they were added (x and v of 3 doubles per
@@ -295,12 +324,27 @@ size_t cs_scene_device_bytes(int np, const double *X0, int nt, const int *tri, i
  * sized for CS_NOALLOC_MAX_VERTICES rows (about 1.2 MB), which every GPU that
  * loads the library holds until the process exits.  Larger systems return
  * CS_ERR_CAPACITY.  The first call on a device looks up that array's device
- * address (make it before any stream capture).  All calls share the array:
- * calls that overlap on the GPU race, so serialise them.  Runs on `stream`
- * (a cudaStream_t, null for the default stream) and waits for it. */
+ * address; make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race, so serialise them.  Runs on
+ * `stream` (a cudaStream_t, null for the default stream); every call copies conv
+ * and iter to the host and waits for the stream before it returns. */
 int cs_solve_cg_noalloc(const int *row_ptr, const int *col_idx, const double *vcrs, const double *vdia,
                         const double *b, double *x, int np, double tol, int maxit, double *conv, int *iter,
                         void *stream);
+
+/* ---- contact log ------------------------------------------------------------------ */
+/* Test facility, off by default: with logging on, every contact resolution
+ * (GetIntermidiateVelocityContactResolved, self_collision_cloth.cpp:355-456, in
+ * cs_step or cs_resolve_contacts) records, for each cloth it resolves, one entry
+ * per detection it runs, in order: kind (0 proximity, 1 swept), the contact count
+ * and a digest of the ordered contact list (FNV-1a 64 over its 32-bit words, 5 per
+ * contact: is_fv and the canonical key in cloth-local ids).  The log of a cloth
+ * holds its last resolution.  Enabling or disabling clears it.  Each logged
+ * detection copies the contact lists to the host, so frames run slower. */
+int cs_contact_log(cs_ctx *ctx, int enable);
+/* The log of cloth `id`: *n entries, up to cap written (CS_ERR_CAPACITY beyond). */
+int cs_contact_log_read(cs_ctx *ctx, int id, int *kind, int *count, unsigned long long *digest, int cap,
+                        int *n);
 
 /* ---- counters ------------------------------------------------------------------ */
 /* Kernel launches issued by this context since creation (for launch accounting). */

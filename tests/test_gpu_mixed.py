@@ -65,31 +65,37 @@ def test_mixed_implicit_accuracy(mctx, oracle_port, name):
 
 
 def test_mixed_frames_contacts(mctx, oracle_port):
-    """Whole frames from oracle states of the folding sheet: positions within
-    MIXED_RTOL and the same contact counts as the FP64 oracle."""
+    """Whole frames from oracle states of the folding sheet: the same ordered
+    contact list in every detection of the frame (contact log), positions within
+    MIXED_RTOL of the FP64 oracle's next frame, and velocities within the same
+    bound as the position change they make over the frame (|dv| dt)."""
     c = fold_scene()
     cid = mctx.add_cloth(c)
     orc = O.OracleCloth(oracle_port, c)
+    mctx.log_contacts(True)
     frame = 0
-    same = 0
-    frames = [30, 34, 38, 45, 60, 90]
-    for f in frames:
-        orc.step(f - frame)
-        frame = f
-        mctx.set_state(cid, orc.x, orc.v)
-        nxt = O.OracleCloth(oracle_port, c)
-        nxt.x, nxt.v = orc.x.copy(), orc.v.copy()
-        sb = nxt.step(1)[0]
-        mctx.step(1)
-        xa, _ = mctx.get_state(cid)
-        sa = mctx.stats(cid)
-        err = np.abs(xa - nxt.x).max() / max(1.0, np.abs(nxt.x).max())
-        print(f"frame {f}: err {err:.2e} prx {sa['n_prx']}/{sb['n_prx']} ccd {sa['n_ccd']}/{sb['n_ccd']}")
-        same += sa["n_prx"] == sb["n_prx"] and sa["n_ccd"] == sb["n_ccd"]
-        assert err <= 1e-3, (f, err)
-        nxt.close()
-    assert same >= len(frames) - 1
-    mctx.remove_cloth(cid)
+    try:
+        for f in [30, 34, 38, 45, 60, 90]:
+            orc.step(f - frame)
+            frame = f
+            mctx.set_state(cid, orc.x, orc.v)
+            nxt = O.OracleCloth(oracle_port, c)
+            nxt.x, nxt.v = orc.x.copy(), orc.v.copy()
+            nxt.log_contacts(True)
+            nxt.step(1)
+            mctx.step(1)
+            xa, va = mctx.get_state(cid)
+            scale = max(1.0, np.abs(nxt.x).max())
+            ex = np.abs(xa - nxt.x).max() / scale
+            ev = np.abs(va - nxt.v).max() * c.params.dt / scale
+            la, lb = mctx.contact_log(cid), nxt.contact_log()
+            print(f"frame {f}: x {ex:.2e} |dv| dt {ev:.2e} detections {len(la)} contacts {sum(n for _, n, _ in la)}")
+            assert la == lb, (f, [(k, n) for k, n, _ in la], [(k, n) for k, n, _ in lb])
+            assert ex <= MIXED_RTOL and ev <= MIXED_RTOL, (f, ex, ev)
+            nxt.close()
+    finally:
+        mctx.log_contacts(False)
+        mctx.remove_cloth(cid)
 
 
 def test_mixed_batch_runs(mctx):

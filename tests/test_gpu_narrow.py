@@ -80,7 +80,10 @@ def test_prx_contacts_fold_probe_scaled(ctx, oracle_port):
 def test_ccd_contacts_crumpled(ctx, oracle_port, seed):
     """CCD contact sets on crumpled sheets moving with random velocities of
     several scales: coplanarity times cross [0, 1] at many pairs, which the FP32
-    no-root certificate in front of the FP64 cubic must never reject."""
+    certificates in front of the FP64 tests (the no-root certificate of the
+    coplanarity cubic for both kinds, the face-vertex sign block) must never
+    reject.  The batch's own contact frames are covered by the contact logs of
+    tests/test_gpu_mixed_batch.py."""
     c = scene.square_cloth(31, 0.5, 0.4, sphere_radius=0.2, clearance=0.01, seed=40 + seed,
                            solver_kind=scene.SOLVER_CG, tol=1e-6, maxit=1000)
     cid = ctx.add_cloth(c)
@@ -88,7 +91,7 @@ def test_ccd_contacts_crumpled(ctx, oracle_port, seed):
     rng = np.random.default_rng(100 + seed)
     x = crumpled(c, seed, amp_xy=0.003 * (1 + seed), amp_z=0.005 * (1 + seed % 3))
     total = 0
-    for scale in (0.05, 0.3, 1.0, 3.0):
+    for scale in (1e-4, 1e-3, 0.05, 0.3, 1.0, 3.0):
         v = rng.normal(0.0, scale, x.size)
         v[2::3] -= 2.0  # a common downward drift, as when falling
         a = ctx.contacts_ccd(cid, x, v, c.params.dt, c.params.contact_clearance)
@@ -98,3 +101,27 @@ def test_ccd_contacts_crumpled(ctx, oracle_port, seed):
     ctx.remove_cloth(cid)
     orc.close()
     assert total > 0
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_ccd_contacts_flat_sheet_crossing(ctx, oracle_port, seed):
+    """A flat sheet (only its 1e-4 jitter off the plane) whose vertices move
+    across their neighbours' face planes by about the jitter: signed heights and
+    coplanarity cubics near zero at nearly every face-vertex pair."""
+    c = scene.square_cloth(41, 0.5, 0.4, sphere_radius=0.2, clearance=0.01, seed=60 + seed,
+                           solver_kind=scene.SOLVER_CG, tol=1e-6, maxit=1000)
+    cid = ctx.add_cloth(c)
+    orc = O.OracleCloth(oracle_port, c)
+    rng = np.random.default_rng(200 + seed)
+    x = c.X0.copy()
+    total = 0
+    for scale in (1e-3, 5e-3, 2e-2):
+        v = np.zeros_like(x)
+        v[2::3] = rng.normal(0.0, scale, x.size // 3) - 1.0
+        v[0::3] = rng.normal(0.0, 0.1 * scale, x.size // 3)
+        a = ctx.contacts_ccd(cid, x, v, c.params.dt, c.params.contact_clearance)
+        b = orc.contacts_ccd(x, v, c.params.dt, c.params.contact_clearance)
+        assert np.array_equal(a, b), (seed, scale, len(a), len(b))
+        total += len(b)
+    ctx.remove_cloth(cid)
+    orc.close()

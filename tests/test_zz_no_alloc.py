@@ -3,8 +3,10 @@ memory (an engine that owns every device allocation, a real-time loop that must
 not enter the CUDA allocator).  The caller hands over the block system already
 in device memory; the entry point keeps its work vectors in a fixed device
 array instead of allocating.  Checked through the C ABI against the context's
-cs_solve_cg on the same system, on two calls in a row, within the parity
-tolerance of the other GPU tests (RTOL relative)."""
+cs_solve_cg and the oracle's Solve_CG on the same system, on two calls in a
+row, within the parity tolerance of the other GPU tests (RTOL relative), and on
+a solve cut off by its iteration cap, where the reference reports the tolerance
+and the cap (matrix_square_sparse.cpp:338-406)."""
 import ctypes
 import json
 import os
@@ -24,8 +26,10 @@ def test_noalloc_cg_matches_context_solve():
     from cloth_sim_self_collision_gb300 import _native as N
     from cloth_sim_self_collision_gb300 import build, scene
     from cloth_sim_self_collision_gb300.context import ClothContext
+    from oracle import oracle as O
 
     build.build()
+    O.build("port")
     L = N.load()
     torch.cuda.set_device(0)
     c = scene.config_small()
@@ -35,6 +39,12 @@ def test_noalloc_cg_matches_context_solve():
     vd, vc, b = ctx.assemble(cid, arr["probe_x"], arr["probe_v"])
     rp, ci = ctx.pattern(cid)
     x_ref, conv_ref, it_ref = ctx.cg(cid, b, 1e-6, 1000)
+    orc = O.OracleCloth(O.OracleLib("port"), c)
+    vdo, vco, bo = orc.assemble(arr["probe_x"], arr["probe_v"])
+    assert np.array_equal(vdo, vd) and np.array_equal(vco, vc) and np.array_equal(bo, b)
+    x_orc, conv_orc, it_orc = orc.cg(b, 1e-6, 1000)
+    x_cut, conv_cut, it_cut = orc.cg(b, 1e-6, 5)
+    assert conv_cut == 1e-6 and it_cut == 5
 
     dev = torch.device("cuda", 0)
     t_rp = torch.from_numpy(rp.astype(np.int32)).to(dev)
@@ -57,6 +67,22 @@ def test_noalloc_cg_matches_context_solve():
         assert np.abs(x - x_ref).max() <= RTOL * scale, (call, np.abs(x - x_ref).max())
         assert abs(it.value - it_ref) <= 1, (call, it.value, it_ref)
         assert abs(conv.value - conv_ref) <= 1e-6 * conv_ref + 1e-300, (call, conv.value, conv_ref)
+        scale = max(1.0, np.abs(x_orc).max())
+        assert np.abs(x - x_orc).max() <= RTOL * scale, (call, np.abs(x - x_orc).max())
+        assert abs(it.value - it_orc) <= 1, (call, it.value, it_orc)
+        assert abs(conv.value - conv_orc) <= 1e-6 * conv_orc + 1e-300, (call, conv.value, conv_orc)
+    # a solve stopped by its cap: conv and iter keep the tolerance and the cap
+    for call in range(2):
+        conv = ctypes.c_double()
+        it = ctypes.c_int()
+        rc = L.cs_solve_cg_noalloc(t_rp.data_ptr(), t_ci.data_ptr(), t_vc.data_ptr(), t_vd.data_ptr(),
+                                   t_b.data_ptr(), t_x.data_ptr(), c.np, 1e-6, 5, ctypes.byref(conv),
+                                   ctypes.byref(it), ctypes.c_void_p(stream))
+        assert rc == N.CS_OK, (call, rc)
+        assert conv.value == 1e-6 and it.value == 5, (call, conv.value, it.value)
+        x = t_x.cpu().numpy()
+        assert np.abs(x - x_cut).max() <= RTOL * max(1.0, np.abs(x_cut).max()), (call, np.abs(x - x_cut).max())
+    orc.close()
     ctx.close()
 
 
