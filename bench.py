@@ -210,7 +210,10 @@ def profiled_replay(ctx, steps, start, profile_names=()):
 
 PROFILED = ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit", "traverse",
             "narrow", "impulse", "pcg", "ilu_factor", "mx_spmv", "mx_update", "mx_direction", "mx_residual",
-            "mx_persist")
+            "mx_persist", "narrow_filter", "narrow_fv", "narrow_ee", "sort")
+
+
+NESTED = ("narrow_filter", "narrow_fv", "narrow_ee")
 
 
 def plain_one_per_launch(cloths, device, steps: int, warmup: int, start, budget_s: float = 8.0) -> dict:
@@ -488,8 +491,10 @@ def native(args):
     # device per processed tile / row; the kernel with the largest share is reported
     # beside it (the FP64 narrow phase is bound by the FP64 pipe, not by HBM).
     prof = head["prof"]
-    top = max(prof, key=lambda k: prof[k][0])
-    total_kernel_ms = sum(v[0] for v in prof.values())
+    # the narrow phase's three kernels are timed both as one class and apart
+    outer = {k: v for k, v in prof.items() if k not in NESTED}
+    top = max(outer, key=lambda k: outer[k][0])
+    total_kernel_ms = sum(v[0] for v in outer.values())
     peaks = read_peaks()
     figs = profile_figures()
     if results["headline"] == "mixed":

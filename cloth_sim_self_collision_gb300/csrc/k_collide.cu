@@ -1013,9 +1013,15 @@ void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* 
   }
   prof_begin(PK_NARROW, s);
   cudaMemsetAsync(C.counters + 6, 0, 2 * sizeof(int), s);
+  prof_begin(PK_NARROW_FILTER, s);
   k_narrow_filter<<<nblk(npairs), kT, 0, s>>>(A, C, ccd, delta_override, npairs);
+  prof_end(PK_NARROW_FILTER, s);
+  prof_begin(PK_NARROW_FV, s);
   k_narrow_fv<<<grid2, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
+  prof_end(PK_NARROW_FV, s);
+  prof_begin(PK_NARROW_EE, s);
   k_narrow_ee<<<grid2, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
+  prof_end(PK_NARROW_EE, s);
   prof_end(PK_NARROW, s);
   g_launches += 3;
 }
@@ -1055,6 +1061,7 @@ void sort_dedupe(const Arena& A, ContactBufs& C, int n, cudaStream_t s) {
     return;
   }
   // lexicographic (k0, k1, k2, k3): stable sort by the low pair, then the high pair
+  prof_begin(PK_SORT, s);
   k_keys_lo<<<nblk(n), kT, 0, s>>>(C, n);
   cub_sort_pairs(C.cub_tmp, C.cub_bytes, C.key_a, C.key_b, C.idx_a, C.idx_b, n, s);
   k_keys_hi<<<nblk(n), kT, 0, s>>>(C, n);
@@ -1065,6 +1072,7 @@ void sort_dedupe(const Arena& A, ContactBufs& C, int n, cudaStream_t s) {
   k_compact<<<nblk(n), kT, 0, s>>>(A, C, n);
   k_segments<<<nblk(n), kT, 0, s>>>(A, C);
   k_counts<<<nblk(A.ni), kT, 0, s>>>(A, C);
+  prof_end(PK_SORT, s);
   g_launches += 7;
 }
 

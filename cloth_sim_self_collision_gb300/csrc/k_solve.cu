@@ -152,16 +152,93 @@ __device__ void copy_matrix(const Arena& A, int v0, int v1) {
   __syncthreads();
 }
 
-// Factorises rows by level; rows after `limit` are left as copied and row
-// `limit` gets its updates only, as when the reference stops after more than
-// ten singular pivots (ilu_sparse.cpp:541-551).
+// Rows with more blocks than this are factorised by one thread (factor_row);
+// grid rows have at most 13.
+constexpr int kRowSlots = 24;
+
+// One row of DoILUDecomp by a warp, the row's blocks staged in shared memory
+// (sm: 9 * (1 + kRowSlots) doubles: D, then the row's slots).  Lanes 0-8 own one
+// entry (r, c) of the 3x3 blocks and apply the updates in the reference's
+// order, entry by entry exactly as factor_row does; the warp syncs between
+// updates because a later update may read a block an earlier one wrote.
+// Returns 1 when the pivot is singular (all lanes).
+__device__ int factor_row_warp(const Arena& A, int i, bool stop_here, double* sm) {
+  const int lane = threadIdx.x & 31;
+  const int r0 = A.row_ptr[i], r1 = A.row_ptr[i + 1], n = r1 - r0;
+  for (int k = lane; k < 9 * (n + 1); k += 32) sm[k] = k < 9 ? A.fdia[9 * (size_t)i + k] : A.fcrs[9 * (size_t)r0 + k - 9];
+  __syncwarp();
+  const int r = lane / 3, c = lane % 3;
+  for (int o = A.fac_ptr[i]; o < A.fac_ptr[i + 1]; o++) {
+    const int s = A.fac_ops[3 * o + 0], ks = A.fac_ops[3 * o + 1], tg = A.fac_ops[3 * o + 2];
+    if (lane < 9) {
+      const double* lik = sm + 9 * (1 + s - r0);
+      const double* ukj = A.fcrs + 9 * (size_t)ks;
+      double* dst = (tg < 0) ? sm : sm + 9 * (1 + tg - r0);
+      dst[r * 3 + c] -= lik[r * 3 + 0] * ukj[c] + lik[r * 3 + 1] * ukj[3 + c] + lik[r * 3 + 2] * ukj[6 + c];
+    }
+    __syncwarp();
+  }
+  double t[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) t[k] = sm[k];
+  __syncwarp();
+  const double det = det33(t);
+  const int singular = fabs(det) > 1.0e-30 ? 0 : 1;
+  if (!singular && !stop_here && lane < 9) {
+    // CalcInvMat3 (ilu_sparse.cpp:76-97) as inv33: entry `lane` of the cofactor inverse
+    double inv[9];
+    inv33(inv, t);
+    double val = inv[0];
+#pragma unroll
+    for (int q = 1; q < 9; q++)
+      if (lane == q) val = inv[q];
+    sm[lane] = val;
+  }
+  __syncwarp();
+  if (!stop_here) {
+    // U <- D^-1 U, three blocks at a time (lanes 9g .. 9g + 8 for block g)
+    const int ds = A.dia_split[i];
+    const int g = lane / 9, e = lane % 9, er = e / 3, ec = e % 3;
+    for (int s0 = ds; s0 < r1; s0 += 3) {
+      const int s = s0 + g;
+      double val = 0.0;
+      const bool mine = g < 3 && s < r1;
+      if (mine) {
+        const double* w = sm + 9 * (1 + s - r0);
+        val = sm[er * 3 + 0] * w[ec] + sm[er * 3 + 1] * w[3 + ec] + sm[er * 3 + 2] * w[6 + ec];
+      }
+      __syncwarp();
+      if (mine) sm[9 * (1 + s - r0) + e] = val;
+      __syncwarp();
+    }
+  }
+  for (int k = lane; k < 9 * (n + 1); k += 32) {
+    if (k < 9)
+      A.fdia[9 * (size_t)i + k] = sm[k];
+    else
+      A.fcrs[9 * (size_t)r0 + k - 9] = sm[k];
+  }
+  __syncwarp();
+  return singular;
+}
+
+// Factorises rows by level, one warp per row; rows after `limit` are left as
+// copied and row `limit` gets its updates only, as when the reference stops
+// after more than ten singular pivots (ilu_sparse.cpp:541-551).
 __device__ void factor_levels(const Arena& A, int inst, int limit) {
+  __shared__ double sm_rows[kSolveThreads / 32][9 * (1 + kRowSlots)];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int l0 = A.lev_off[inst], l1 = A.lev_off[inst + 1];
   for (int l = l0; l < l1; l++) {
-    for (int k = A.lev_ptr[l] + threadIdx.x; k < A.lev_ptr[l + 1]; k += blockDim.x) {
+    for (int k = A.lev_ptr[l] + warp; k < A.lev_ptr[l + 1]; k += nw) {
       const int i = A.lev_rows[k];
       if (i > limit) continue;
-      A.sing[i] = factor_row(A, i, i == limit);
+      if (A.row_ptr[i + 1] - A.row_ptr[i] <= kRowSlots) {
+        const int sg = factor_row_warp(A, i, i == limit, sm_rows[warp]);
+        if (lane == 0) A.sing[i] = sg;
+      } else if (lane == 0) {
+        A.sing[i] = factor_row(A, i, i == limit);
+      }
     }
     __syncthreads();
   }
@@ -194,43 +271,59 @@ __global__ void __launch_bounds__(kSolveThreads) k_ilu_factor(Arena A, const int
   if (threadIdx.x == 0) A.st[inst].ilu_singular = nsing > 10 ? 11 : nsing;
 }
 
+// t -= sum over the slots [s0, s1) of B_s z_col(s), in slot order, by a warp:
+// lane j forms slot j's three row products (B[r][0] y0 + B[r][1] y1 + B[r][2] y2,
+// the reference's grouping), then every lane subtracts them in slot order
+__device__ __forceinline__ void row_sweep_sub(const Arena& A, const double* z, int s0, int s1, double t[3]) {
+  const int lane = threadIdx.x & 31;
+  for (int base = s0; base < s1; base += 32) {
+    const int s = base + lane;
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    if (s < s1) {
+      const int j = A.col_idx[s];
+      const double* b9 = A.fcrs + 9 * (size_t)s;
+      const double y0 = z[3 * j + 0], y1 = z[3 * j + 1], y2 = z[3 * j + 2];
+      d0 = b9[0] * y0 + b9[1] * y1 + b9[2] * y2;
+      d1 = b9[3] * y0 + b9[4] * y1 + b9[5] * y2;
+      d2 = b9[6] * y0 + b9[7] * y1 + b9[8] * y2;
+    }
+    const int m = min(32, s1 - base);
+    for (int q = 0; q < m; q++) {
+      t[0] -= __shfl_sync(0xffffffffu, d0, q);
+      t[1] -= __shfl_sync(0xffffffffu, d1, q);
+      t[2] -= __shfl_sync(0xffffffffu, d2, q);
+    }
+  }
+}
+
 // z <- (LU)^-1 z in place: forward sweep by levels, then backward sweep by
-// levels (ilu_sparse.cpp:185-215, 295-324)
+// levels (ilu_sparse.cpp:185-215, 295-324), one warp per row
 __device__ void ilu_apply(const Arena& A, int inst, double* z) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int l = A.lev_off[inst]; l < A.lev_off[inst + 1]; l++) {
-    for (int k = A.lev_ptr[l] + threadIdx.x; k < A.lev_ptr[l + 1]; k += blockDim.x) {
+    for (int k = A.lev_ptr[l] + warp; k < A.lev_ptr[l + 1]; k += nw) {
       const int i = A.lev_rows[k];
-      double t0 = z[3 * i + 0], t1 = z[3 * i + 1], t2 = z[3 * i + 2];
-      for (int s = A.row_ptr[i]; s < A.dia_split[i]; s++) {
-        const int j = A.col_idx[s];
-        const double* l9 = A.fcrs + 9 * (size_t)s;
-        const double y0 = z[3 * j + 0], y1 = z[3 * j + 1], y2 = z[3 * j + 2];
-        t0 -= l9[0] * y0 + l9[1] * y1 + l9[2] * y2;
-        t1 -= l9[3] * y0 + l9[4] * y1 + l9[5] * y2;
-        t2 -= l9[6] * y0 + l9[7] * y1 + l9[8] * y2;
+      double t[3] = {z[3 * i + 0], z[3 * i + 1], z[3 * i + 2]};
+      row_sweep_sub(A, z, A.row_ptr[i], A.dia_split[i], t);
+      if (lane == 0) {
+        const double* d = A.fdia + 9 * (size_t)i;
+        z[3 * i + 0] = d[0] * t[0] + d[1] * t[1] + d[2] * t[2];
+        z[3 * i + 1] = d[3] * t[0] + d[4] * t[1] + d[5] * t[2];
+        z[3 * i + 2] = d[6] * t[0] + d[7] * t[1] + d[8] * t[2];
       }
-      const double* d = A.fdia + 9 * (size_t)i;
-      z[3 * i + 0] = d[0] * t0 + d[1] * t1 + d[2] * t2;
-      z[3 * i + 1] = d[3] * t0 + d[4] * t1 + d[5] * t2;
-      z[3 * i + 2] = d[6] * t0 + d[7] * t1 + d[8] * t2;
     }
     __syncthreads();
   }
   for (int l = A.blev_off[inst]; l < A.blev_off[inst + 1]; l++) {
-    for (int k = A.blev_ptr[l] + threadIdx.x; k < A.blev_ptr[l + 1]; k += blockDim.x) {
+    for (int k = A.blev_ptr[l] + warp; k < A.blev_ptr[l + 1]; k += nw) {
       const int i = A.blev_rows[k];
-      double t0 = z[3 * i + 0], t1 = z[3 * i + 1], t2 = z[3 * i + 2];
-      for (int s = A.dia_split[i]; s < A.row_ptr[i + 1]; s++) {
-        const int j = A.col_idx[s];
-        const double* u = A.fcrs + 9 * (size_t)s;
-        const double y0 = z[3 * j + 0], y1 = z[3 * j + 1], y2 = z[3 * j + 2];
-        t0 -= u[0] * y0 + u[1] * y1 + u[2] * y2;
-        t1 -= u[3] * y0 + u[4] * y1 + u[5] * y2;
-        t2 -= u[6] * y0 + u[7] * y1 + u[8] * y2;
+      double t[3] = {z[3 * i + 0], z[3 * i + 1], z[3 * i + 2]};
+      row_sweep_sub(A, z, A.dia_split[i], A.row_ptr[i + 1], t);
+      if (lane == 0) {
+        z[3 * i + 0] = t[0];
+        z[3 * i + 1] = t[1];
+        z[3 * i + 2] = t[2];
       }
-      z[3 * i + 0] = t0;
-      z[3 * i + 1] = t1;
-      z[3 * i + 2] = t2;
     }
     __syncthreads();
   }

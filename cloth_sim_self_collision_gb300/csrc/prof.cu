@@ -10,7 +10,8 @@ const char* const kProfNames[PK_COUNT] = {"tri_elements", "slot_reduce", "rhs", 
                                           "pcg",          "cg_spmv",     "cg_update", "cg_direction",
                                           "refit",        "traverse",    "narrow",    "impulse",
                                           "mx_spmv",      "mx_update",   "mx_direction", "mx_residual",
-                                          "mx_persist"};
+                                          "mx_persist",   "narrow_filter", "narrow_fv", "narrow_ee",
+                                          "sort"};
 
 namespace {
 struct Pending {

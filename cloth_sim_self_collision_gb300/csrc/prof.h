@@ -23,6 +23,10 @@ enum ProfKernel {
   PK_MX_DIRECTION,
   PK_MX_RESIDUAL,
   PK_MX_PERSIST,
+  PK_NARROW_FILTER,
+  PK_NARROW_FV,
+  PK_NARROW_EE,
+  PK_SORT,
   PK_COUNT
 };
 
