@@ -403,6 +403,104 @@ __device__ __forceinline__ bool fv_sign_reject32(V3<double> e1, V3<double> e2, V
   return pos || neg;
 }
 
+// Closest points of segments a0 a1 and b0 b1 (FP32, clamped): the vector from
+// the point on a to the point on b.  Only a direction for the certificate below.
+__device__ __forceinline__ void seg_seg_dir32(const float a0[3], const float a1[3], const float b0[3],
+                                              const float b1[3], float d[3]) {
+  float u[3], v[3], w[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    u[k] = a1[k] - a0[k];
+    v[k] = b1[k] - b0[k];
+    w[k] = a0[k] - b0[k];
+  }
+  const float A = u[0] * u[0] + u[1] * u[1] + u[2] * u[2], B = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+  const float C = v[0] * v[0] + v[1] * v[1] + v[2] * v[2], D = u[0] * w[0] + u[1] * w[1] + u[2] * w[2];
+  const float E = v[0] * w[0] + v[1] * w[1] + v[2] * w[2];
+  const float den = A * C - B * B;
+  float sa = (den > 1e-12f * A * C) ? (B * E - C * D) / den : 0.f;
+  sa = fminf(fmaxf(sa, 0.f), 1.f);
+  float sb = C > 0.f ? (B * sa + E) / C : 0.f;
+  if (sb < 0.f) {
+    sb = 0.f;
+    sa = A > 0.f ? fminf(fmaxf(-D / A, 0.f), 1.f) : 0.f;
+  } else if (sb > 1.f) {
+    sb = 1.f;
+    sa = A > 0.f ? fminf(fmaxf((B - D) / A, 0.f), 1.f) : 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) d[k] = (b0[k] + sb * v[k]) - (a0[k] + sa * u[k]);
+}
+
+// True when IsContact_EE_CCD's distance test (bvh_aabb.cpp:786-791: the edges'
+// distance at the coplanarity time must not exceed 1e-2) certainly rejects,
+// for edges p (p0, p1) and q (q0, q1) moving from s to e.  At every time in
+// [0, 1] an edge lies in the convex hull of its four start and end points, so
+// a separating axis d along which the two hulls are more than dmax apart bounds
+// the distance the reference computes there from below: its closest points lie
+// on the segments whenever both ratios pass, and its parallel-edge branch
+// (|vp x vq| < 1e-10) measures a line distance that undercuts the segment
+// distance by at most 1e-10 over the length of an edge.  The certificate
+// therefore requires both edges to be at least 1e-3 m long at the start and the
+// end without turning over (start and end directions with a positive dot
+// product, so no edge degenerates in between) and keeps a margin of 1e-6 m,
+// which also covers the FP64 rounding of the reference's interpolation and
+// distance.  The points enter as FP64 differences from p0s rounded to FP32, and
+// each projection carries an error bound.
+__device__ __forceinline__ bool ee_ccd_far32(V3<double> p0s, V3<double> p1s, V3<double> q0s, V3<double> q1s,
+                                             V3<double> p0e, V3<double> p1e, V3<double> q0e, V3<double> q1e,
+                                             double dmax) {
+  {
+    // edge vectors at the start and the end (FP64 differences, rounded)
+    const F3E es[2] = {f3e_round(p1s - p0s), f3e_round(q1s - q0s)};
+    const F3E ee[2] = {f3e_round(p1e - p0e), f3e_round(q1e - q0e)};
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const float ls = es[k].v[0] * es[k].v[0] + es[k].v[1] * es[k].v[1] + es[k].v[2] * es[k].v[2];
+      const float le = ee[k].v[0] * ee[k].v[0] + ee[k].v[1] * ee[k].v[1] + ee[k].v[2] * ee[k].v[2];
+      const float se = es[k].v[0] * ee[k].v[0] + es[k].v[1] * ee[k].v[1] + es[k].v[2] * ee[k].v[2];
+      // 1.1e-6: (1e-3 m)^2 with room for the rounding of these sums
+      if (!(ls > 1.1e-6f) || !(le > 1.1e-6f) || !(se > 1.0e-3f * sqrtf(ls * le))) return false;
+    }
+  }
+  const F3E P[4] = {f3e_round(p0s - p0s), f3e_round(p1s - p0s), f3e_round(p0e - p0s), f3e_round(p1e - p0s)};
+  const F3E Q[4] = {f3e_round(q0s - p0s), f3e_round(q1s - p0s), f3e_round(q0e - p0s), f3e_round(q1e - p0s)};
+  // direction: closest points of the edges halfway through the motion
+  float a0[3], a1[3], b0[3], b1[3], d[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    a0[k] = 0.5f * (P[0].v[k] + P[2].v[k]);
+    a1[k] = 0.5f * (P[1].v[k] + P[3].v[k]);
+    b0[k] = 0.5f * (Q[0].v[k] + Q[2].v[k]);
+    b1[k] = 0.5f * (Q[1].v[k] + Q[3].v[k]);
+  }
+  seg_seg_dir32(a0, a1, b0, b1, d);
+  const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  if (!(dd > 0.f) || !isfinite(dd)) return false;
+  F3E dv;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    dv.v[k] = d[k];
+    dv.e[k] = 0.f;  // any axis will do: d is taken as exact
+  }
+  float pmax = -INFINITY, pmin = INFINITY, qmax = -INFINITY, qmin = INFINITY;
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    float t, e;
+    f3e_dot(P[m], dv, t, e);
+    pmax = fmaxf(pmax, t + e);
+    pmin = fminf(pmin, t - e);
+    f3e_dot(Q[m], dv, t, e);
+    qmax = fmaxf(qmax, t + e);
+    qmin = fminf(qmin, t - e);
+  }
+  // |d| from above, and the gap from below (each subtraction rounded down)
+  const float dlen = __fmul_ru(__fsqrt_ru(dd), 1.0000005f);
+  const float need = __fmul_ru(__double2float_ru(dmax + 1.0e-6), dlen);
+  const float gap = fmaxf(__fsub_rd(qmin, pmax), __fsub_rd(pmin, qmax));
+  return gap > need;
+}
+
 // ---------------------------------------------------------------------------
 // elementary contact tests (bvh_aabb.cpp:392-438, 666-793)
 // ---------------------------------------------------------------------------

@@ -507,6 +507,8 @@ __global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, c
     } else {
       const V3<double> p0e = end_pos(xs, vs, i0, P.dt), p1e = end_pos(xs, vs, i1, P.dt);
       const V3<double> q0e = end_pos(xs, vs, j0, P.dt), q1e = end_pos(xs, vs, j1, P.dt);
+      // the edges stay more than the test's 1e-2 apart over the whole motion
+      if (ee_ccd_far32(p0, p1, q0, q1, p0e, p1e, q0e, q1e, 1.0e-2)) continue;
       {
         // no coplanarity in [0, 1]: the vectors coplanar_time forms, in FP64 as it does
         const V3<double> x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0;
