@@ -41,7 +41,8 @@ EXPORTS = [
     "cs_server_create", "cs_server_submit", "cs_server_wait", "cs_server_release", "cs_server_drain",
     "cs_server_get_stats", "cs_server_last_error", "cs_server_destroy", "cs_scene_device_bytes",
     "cs_vertex_normals", "cs_contact_log", "cs_contact_log_read", "cs_matvec", "cs_set_matrix", "cs_ilu_solve",
-    "cs_distance_fv", "cs_distance_ee", "cs_coplanar_time", "cs_last_residual",
+    "cs_distance_fv", "cs_distance_ee", "cs_coplanar_time", "cs_last_residual", "cs_set_frame_mode",
+    "cs_frame_counts",
 ]
 
 
@@ -204,6 +205,9 @@ def load(path: str | None = None, build_if_missing: bool = False):
     f("cs_scene_device_bytes", ctypes.c_size_t, i, _D, i, _I, i, _I, P)
     f("cs_vertex_normals", i, _V, i, _D, _D)
     f("cs_contact_log", i, _V, i)
+    f("cs_set_frame_mode", i, _V, i)
+    LL = ctypes.POINTER(ctypes.c_longlong)
+    f("cs_frame_counts", i, _V, LL, LL, LL, LL)
     f("cs_matvec", i, _V, i, d, _D, d, _D)
     f("cs_last_residual", i, _V, i, _D)
     f("cs_set_matrix", i, _V, i, _D, _D)

@@ -26,7 +26,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-re
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-pthread"]
 SOURCES = ["topology.cpp", "prof.cu", "k_assemble.cu", "k_solve.cu", "k_mixed.cu", "k_collide.cu", "api.cu",
-           "k_noalloc.cu", "serve.cu"]
+           "k_noalloc.cu", "serve.cu", "frame_graph.cu"]
 
 
 def nvcc() -> str:

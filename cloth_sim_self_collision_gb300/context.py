@@ -122,6 +122,16 @@ class ClothContext:
         self._ck(self.L.cs_profile_read(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def frame_mode(self, graph: bool):
+        """Frames as one captured CUDA graph each (True, the default) or host-driven."""
+        self._ck(self.L.cs_set_frame_mode(self.h, 1 if graph else 0))
+
+    def frame_counts(self) -> dict:
+        """Graph frames, host-driven frames, graph captures, graph frames re-run host-driven."""
+        v = [ctypes.c_longlong() for _ in range(4)]
+        self._ck(self.L.cs_frame_counts(self.h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("graph_frames", "host_frames", "captures", "overflows"), (x.value for x in v)))
+
     def log_contacts(self, enable: bool = True):
         """Record, per detection of each cloth's next contact resolution, (kind,
         count, digest of the ordered contact list)."""

@@ -56,7 +56,7 @@ void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t
   C.ce = m.alloc<int>(5 * (size_t)cand_cap);
   C.ce_inst_lo = m.alloc<int>(A.ni);
   C.ce_inst_hi = m.alloc<int>(A.ni);
-  C.counters = m.alloc<int>(8);
+  C.counters = m.alloc<int>(16);
   C.level = m.alloc<int>(cand_cap);
   C.order = m.alloc<int>(cand_cap);
   C.lev_cnt = m.alloc<int>((size_t)cand_cap + A.ni + 1);
@@ -68,13 +68,13 @@ void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t
   C.cub_bytes = cub_sort_bytes(std::max(cand_cap, A.nv));
   C.cub_tmp = m.alloc<char>(C.cub_bytes);
   CK(cudaMemsetAsync(C.vstamp, 0xff, sizeof(int) * (size_t)A.nv, s));
-  CK(cudaMemsetAsync(C.counters, 0, sizeof(int) * 8, s));
+  CK(cudaMemsetAsync(C.counters, 0, sizeof(int) * 16, s));
 }
 
 void alloc_contacts(cs_ctx* c, int pair_cap, int cand_cap, int q_fv = -1, int q_ee = -1) {
+  graph_release(c);  // the graph holds the old buffers' addresses
   free_contacts(c);
   alloc_contacts_into(c->A, c->C, c->cmem, c->stream, pair_cap, cand_cap, q_fv, q_ee);
-  c->token = 0;
 }
 
 // Packs the cloths cl (in this order) into a fresh device arena o on stream s:
@@ -301,6 +301,8 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
   A.inzone = m.alloc<int>(NV);
   CK(cudaMemsetAsync(A.inzone, 0, sizeof(int) * (size_t)std::max(NV, 1), s));
   o.d_list = m.alloc<int>(std::max(ni, 1));
+  A.ctl = m.alloc<FrameCtl>(1);
+  CK(cudaMemsetAsync(A.ctl, 0, sizeof(FrameCtl), s));
   // mixed precision: SELL-32 slices of every cloth's rows (32 rows per slice,
   // padded to the widest row with zero blocks pointing at the slice's own row)
   {
@@ -402,6 +404,7 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
 
 // Makes o the context's arena; the previous arena's buffers end up in o.
 void install(cs_ctx* c, ArenaSet& o) {
+  graph_release(c);
   std::swap(c->A, o.A);
   std::swap(c->C, o.C);
   std::swap(c->mem, o.mem);
@@ -417,7 +420,6 @@ void install(cs_ctx* c, ArenaSet& o) {
   std::swap(c->hst, o.hst);
   c->dead.assign(c->order.size(), 0);
   for (size_t i = 0; i < c->order.size(); i++) c->dead[i] = c->cloths[c->order[i]]->stats.diverged;
-  c->token = 0;
   c->last_ncand = 0;
   c->last_nce = 0;
   c->dirty = false;
@@ -647,6 +649,7 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
     }
     if (ok) {
       const int ncand = cnt[1];
+      c->max_ncand = std::max<long long>(c->max_ncand, ncand);
       sort_dedupe(c->A, c->C, ncand, s);
       CK(cudaGetLastError());
       int total = 0;
@@ -704,6 +707,7 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
     launch_traverse(c->A, c->C, s);
   }
   const int ncand = cnt[1];
+  c->max_ncand = std::max<long long>(c->max_ncand, ncand);
   sort_dedupe(c->A, c->C, ncand, s);
   CK(cudaGetLastError());
   int total = 0;
@@ -721,8 +725,7 @@ int detect(cs_ctx* c, int ccd, const double* xs, const double* vs, double delta_
 }
 
 void impulses(cs_ctx* c, int ccd, const double* xs, double* vs) {
-  c->token++;
-  launch_impulses(c->A, c->C, ccd, xs, vs, c->token, c->stream);
+  launch_impulses(c->A, c->C, ccd, xs, vs, c->stream);
 }
 
 void drop_dead(const cs_ctx* c, std::vector<int>& phase, std::vector<int>& applied) {
@@ -814,7 +817,7 @@ std::vector<int> resolve(cs_ctx* c, const std::vector<int>& act) {
       for (int i = 0; i < ni; i++) work |= phase[i] != 0;
       if (!work) break;
       launch_riz_add(A, c->C, nce, c->stream);
-      riz_apply(A, c->C, A.x1, A.v, A.v0, c->stream);
+      c->max_zone = std::max<long long>(c->max_zone, riz_apply(A, c->C, A.x1, A.v, A.v0, c->stream));
     }
   }
   for (int i = 0; i < ni; i++)
@@ -830,9 +833,22 @@ void update_velocity(cs_ctx* c, const std::vector<int>& act) {
 }
 
 // one frame for the cloths in act (StepTime, self_contact_sparse/main.cpp:213-263)
+// whether the next frame can run as a captured graph: not while per-kernel
+// timing or the contact log need the host between launches, nor on the
+// launch-per-iteration mixed solve
+bool graph_ok(const cs_ctx* c, const std::vector<int>& act) {
+  if (!c->graph_mode || c->A.ni == 0 || prof_enabled() || c->log_on) return false;
+  if (c->precision == CS_PREC_MIXED && !c->mx_persistent) return false;
+  for (int a : act)
+    if (a) return true;
+  return false;
+}
+
 void frame(cs_ctx* c, const std::vector<int>& act_in) {
   const Arena& A = c->A;
   const std::vector<int> act = live(c, act_in);
+  if (graph_ok(c, act) && graph_frame(c, act)) return;
+  c->host_frames++;
   CK(cudaMemcpyAsync(A.x1, A.x, sizeof(double) * 3 * (size_t)A.nv, cudaMemcpyDeviceToDevice, c->stream));
   implicit(c, act);
   pull_states(c);
@@ -976,6 +992,10 @@ void cs_destroy(cs_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  graph_release(c);
+  if (c->gsave) cudaFree(c->gsave);
+  for (cudaStream_t g : c->gstream)
+    if (g) cudaStreamDestroy(g);
   c->mem.release();
   c->cmem.release();
   cudaStreamDestroy(c->stream);
@@ -989,6 +1009,7 @@ void* cs_stream(const cs_ctx* c) { return c ? (void*)c->stream : nullptr; }
 int cs_set_precision(cs_ctx* c, int precision) {
   return guarded(c, [&] {
     if (precision != CS_PREC_FP64 && precision != CS_PREC_MIXED) throw ArgError("unknown precision");
+    graph_release(c);
     c->precision = precision;
   });
 }
@@ -1031,6 +1052,7 @@ int cs_set_params(cs_ctx* c, int id, const cs_params* prm) {
   return guarded(c, [&] {
     if (!prm) throw ArgError("null params");
     Cloth& cl = cloth_at(c, id);
+    graph_release(c);  // solver lists and caps are part of the graph
     if (prm->solver_kind != cl.prm.solver_kind) {
       // the ILU schedule is part of the topology
       save_states(c);
@@ -1588,6 +1610,24 @@ int cs_coplanar_time(cs_ctx* c, int n, const double* s0, const double* e0, doubl
                        [&](std::vector<double*>& i, std::vector<double*>& o) {
                          launch_coplanar_time(n, i[0], i[1], o[0], c->stream);
                        });
+}
+
+int cs_set_frame_mode(cs_ctx* c, int mode) {
+  return guarded(c, [&] {
+    if (mode != CS_FRAME_HOST && mode != CS_FRAME_GRAPH) throw ArgError("unknown frame mode");
+    c->graph_mode = mode == CS_FRAME_GRAPH;
+    if (!c->graph_mode) graph_release(c);
+  });
+}
+
+int cs_frame_counts(cs_ctx* c, long long* graph_frames, long long* host_frames, long long* captures,
+                    long long* overflows) {
+  return guarded(c, [&] {
+    if (graph_frames) *graph_frames = c->g_frames;
+    if (host_frames) *host_frames = c->host_frames;
+    if (captures) *captures = c->g_captures;
+    if (overflows) *overflows = c->g_overflows;
+  });
 }
 
 int cs_contact_log(cs_ctx* c, int enable) {

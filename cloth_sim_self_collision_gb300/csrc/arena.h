@@ -58,6 +58,27 @@ struct InstState {
   int istop;
   int bjac;          // the inner solve runs on the block-Jacobi-scaled matrix
   float alpha32, beta32;
+  // frame control on the device (a frame captured in a CUDA graph): the cloth
+  // takes part in this frame (want), is still in the contact loop of
+  // GetIntermidiateVelocityContactResolved (phase), got an impulse (applied);
+  // and the frame's contact counters (cs_stats)
+  int want, phase, applied;
+  int st_prx, st_ccd[5], st_ccd_passes, st_riz_passes, st_riz_last, st_riz_total, st_riz_nodes;
+};
+
+// Device-side state of a frame captured in a CUDA graph.  The loops of
+// GetIntermidiateVelocityContactResolved (self_collision_cloth.cpp:398-455:
+// up to 5 CCD passes, up to 100 impact-zone passes) and of the solvers run as
+// conditional graph nodes whose conditions kernels set from these counters.
+struct FrameCtl {
+  int ccd_pass;     // CCD passes run in this frame
+  int riz_pass;     // impact-zone passes run
+  int cycle;        // refinement cycles (mixed) / CG iterations (FP64)
+  int overflow;     // a fixed-size buffer overflowed (the host re-runs the frame)
+  int last_ncand;   // candidates of the last detection (kept for the incremental one)
+  int last_nce;     // contacts of the last detection
+  int token;        // stamp of the impulse level schedule (host and graph frames share it)
+  int pad;
 };
 
 struct Arena {
@@ -137,6 +158,7 @@ struct Arena {
   // the bits of positive floats) for the choice of preconditioner
   unsigned* dg_range = nullptr;
   unsigned int* grid_bar = nullptr; // [0] arrivals, [1] generation, [2] gave up, [3] cloths still iterating
+  FrameCtl* ctl = nullptr;          // frame control on the device
 };
 
 // scratch for the contact pipeline (grown on demand)
@@ -155,7 +177,9 @@ struct ContactBufs {
   int* ce_inst_lo = nullptr;  // per cloth segment of ce
   int* ce_inst_hi = nullptr;
   int* counters = nullptr;    // [0] pairs, [1] candidates, [2] contacts, [3] overflow flag,
-                              // [6] / [7] face-vertex / edge-edge tests queued
+                              // [4] zone members, [5] kept candidates, [6] / [7] face-vertex /
+                              // edge-edge tests queued, [8] / [9] sorted candidates / zone
+                              // members of a graph frame
   int* level = nullptr;       // impulse level per contact
   int* order = nullptr;       // contacts grouped by level
   int* lev_cnt = nullptr;     // per cloth: level count (then offsets)

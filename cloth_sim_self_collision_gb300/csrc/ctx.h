@@ -98,7 +98,6 @@ struct cs_ctx {
   std::vector<int> voff, toff, boff, noff, qoff;
   std::vector<int> solver;  // per slot
   int* d_list = nullptr;    // scratch list of cloth slots
-  int token = 0;
   int last_ncand = 0;  // candidates of the last detection (kept in C.cand)
   int last_nce = 0;    // contacts of the last detection (in C.ce)
   std::vector<cs::InstState> hst;
@@ -122,6 +121,21 @@ struct cs_ctx {
   };
   bool log_on = false;
   std::map<int, std::vector<LogEntry>> clog;
+  // largest candidate and zone-member counts of the host-driven detections
+  // (the padded sort sizes of a frame graph are chosen from them)
+  long long max_ncand = 0, max_zone = 0;
+  // frame graph (frame_graph.cu): on by default; its executable, capture
+  // streams, fixed sizes, static solver lists, start-state snapshot, counters
+  bool graph_mode = true;
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t gstream[2] = {nullptr, nullptr};
+  int g_scand = 0, g_szone = 0, g_cg_cap = 0;
+  bool g_cg_serial = false;
+  std::vector<int> g_ilu;
+  int* g_ilu_list = nullptr;
+  double* gsave = nullptr;
+  size_t gsave_n = 0;
+  long long g_frames = 0, g_captures = 0, g_overflows = 0, host_frames = 0;
 };
 
 namespace cs {
@@ -143,6 +157,12 @@ void install(cs_ctx* c, ArenaSet& o);
 void frame(cs_ctx* c, const std::vector<int>& act);
 // maps an exception from the host layer to a CS_* status and records its message
 int status_of(const std::exception& e, std::string* msg);
+// frame graph (frame_graph.cu): capture for the current arena, release, and one
+// frame through it (false: a fixed size overflowed and the start state was
+// restored, so the caller runs the frame host-driven)
+void graph_capture(cs_ctx* c);
+void graph_release(cs_ctx* c);
+bool graph_frame(cs_ctx* c, const std::vector<int>& act);
 
 }  // namespace host
 }  // namespace cs

@@ -162,9 +162,7 @@ __device__ __forceinline__ void load_box32(const float* src, float* b) {
   }
 }
 
-__global__ void k_traverse(Arena A, ContactBufs C) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= A.nt) return;
+__device__ __forceinline__ void traverse_tri(const Arena& A, const ContactBufs& C, int t) {
   const int inst = A.tinst[t];
   if (!A.active[inst] || A.st[inst].diverged) return;
   const int la = A.tri_leaf[t];
@@ -204,12 +202,16 @@ __global__ void k_traverse(Arena A, ContactBufs C) {
   }
 }
 
+__global__ void k_traverse(Arena A, ContactBufs C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < A.nt) traverse_tri(A, C, t);
+}
+
 // every overlapping leaf pair with a dirty triangle, oriented by leaf order; a
 // pair of two dirty triangles is emitted by its left one
 // (overlaps on both sides are walked here: the blow-up limit is doubled)
-__global__ void k_traverse_dirty(Arena A, ContactBufs C) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= A.nt || !A.tdirty[t]) return;
+__device__ __forceinline__ void traverse_dirty_tri(const Arena& A, const ContactBufs& C, int t) {
+  if (!A.tdirty[t]) return;
   const int inst = A.tinst[t];
   if (!A.active[inst] || A.st[inst].diverged) return;
   const int la = A.tri_leaf[t];
@@ -251,6 +253,11 @@ __global__ void k_traverse_dirty(Arena A, ContactBufs C) {
       k++;
     }
   }
+}
+
+__global__ void k_traverse_dirty(Arena A, ContactBufs C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < A.nt) traverse_dirty_tri(A, C, t);
 }
 
 // candidates of the previous detection whose pair has no dirty triangle
@@ -348,13 +355,11 @@ __device__ __forceinline__ void enqueue(const ContactBufs& C, int kind, int pid,
   C.queue[kind][slot] = make_int2(pid, test);
 }
 
-__global__ void __launch_bounds__(kT) k_narrow_filter(Arena A, ContactBufs C, int ccd, double delta_override,
-                                                      int npairs) {
+__device__ __forceinline__ void narrow_filter_pair(const Arena& A, const ContactBufs& C, int ccd,
+                                                   double delta_override, int pid) {
   // the 9 edge pairs of a triangle pair (kEE), as compile-time indices
   constexpr int kE[9][4] = {{0, 1, 0, 1}, {0, 1, 1, 2}, {0, 1, 2, 0}, {1, 2, 0, 1}, {1, 2, 1, 2},
                             {1, 2, 2, 0}, {2, 0, 0, 1}, {2, 0, 1, 2}, {2, 0, 2, 0}};
-  const int pid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pid >= npairs) return;
   const int2 pr = C.pairs[pid];
   const int na = pr.x, nb = pr.y;
   const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
@@ -440,6 +445,19 @@ __global__ void __launch_bounds__(kT) k_narrow_filter(Arena A, ContactBufs C, in
   }
 }
 
+__global__ void __launch_bounds__(kT) k_narrow_filter(Arena A, ContactBufs C, int ccd, double delta_override,
+                                                      int npairs) {
+  const int pid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pid < npairs) narrow_filter_pair(A, C, ccd, delta_override, pid);
+}
+
+// the same over the pair count the broad phase left on the device (grid-stride)
+__global__ void __launch_bounds__(kT) k_narrow_filter_dev(Arena A, ContactBufs C, int ccd, double delta_override) {
+  const int n = min(__ldcg(&C.counters[0]), C.pair_cap);
+  for (int pid = blockIdx.x * blockDim.x + threadIdx.x; pid < n; pid += gridDim.x * blockDim.x)
+    narrow_filter_pair(A, C, ccd, delta_override, pid);
+}
+
 // pass 2, face-vertex tests (grid-stride over their queue)
 __global__ void k_narrow_fv(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs,
                             double delta_override) {
@@ -507,14 +525,14 @@ __global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, c
     } else {
       const V3<double> p0e = end_pos(xs, vs, i0, P.dt), p1e = end_pos(xs, vs, i1, P.dt);
       const V3<double> q0e = end_pos(xs, vs, j0, P.dt), q1e = end_pos(xs, vs, j1, P.dt);
-      // the edges stay more than the test's 1e-2 apart over the whole motion
-      if (ee_ccd_far32(p0, p1, q0, q1, p0e, p1e, q0e, q1e, 1.0e-2)) continue;
       {
         // no coplanarity in [0, 1]: the vectors coplanar_time forms, in FP64 as it does
         const V3<double> x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0;
         const V3<double> v1 = (p1e - p0e) - x1, v2 = (q0e - p0e) - x2, v3 = (q1e - p0e) - x3;
         if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
       }
+      // the edges stay more than the test's 1e-2 apart over the whole motion
+      if (ee_ccd_far32(p0, p1, q0, q1, p0e, p1e, q0e, q1e, 1.0e-2)) continue;
       count_fp64_test(A, 5);
       if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, p0e, p1e, q0e, q1e)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
     }
@@ -658,9 +676,12 @@ __global__ void k_counts(Arena A, ContactBufs C) {
 
 // ---- impulses (self_collision_cloth.cpp:20-212) ------------------------------
 // levels of the sequential sweep, one thread per cloth
-__global__ void k_impulse_levels(Arena A, ContactBufs C, int token) {
+__global__ void k_token_next(Arena A) { A.ctl->token++; }
+
+__global__ void k_impulse_levels(Arena A, ContactBufs C) {
   const int inst = blockIdx.x * blockDim.x + threadIdx.x;
   if (inst >= A.ni) return;
+  const int token = A.ctl->token;
   A.st[inst].nlev = 0;
   if (!A.active[inst]) return;
   const int lo = C.ce_inst_lo[inst], hi = C.ce_inst_hi[inst];
@@ -870,9 +891,8 @@ __global__ void k_riz_collect(Arena A, ContactBufs C, int* count) {
 
 // per zone: centroid, mean velocity, angular momentum and the reference's
 // "inertia" (diagonal |v|^2 - q_i^2), all summed over members in ascending order
-__global__ void k_riz_stats(Arena A, ContactBufs C, int n, const double* xs, const double* v0s) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__device__ __forceinline__ void riz_stats_one(const Arena& A, const ContactBufs& C, int i, int n, const double* xs,
+                                              const double* v0s) {
   const unsigned long long* z = C.zkey2;
   const unsigned root = (unsigned)(z[i] >> 32);
   if (i > 0 && (unsigned)(z[i - 1] >> 32) == root) return;
@@ -931,9 +951,12 @@ __global__ void k_riz_stats(Arena A, ContactBufs C, int n, const double* xs, con
   rec[8] = Iv[6] * L.x + Iv[7] * L.y + Iv[8] * L.z;
 }
 
-__global__ void k_riz_velocity(ContactBufs C, int n, const double* xs, double* vs) {
+__global__ void k_riz_stats(Arena A, ContactBufs C, int n, const double* xs, const double* v0s) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i < n) riz_stats_one(A, C, i, n, xs, v0s);
+}
+
+__device__ __forceinline__ void riz_velocity_one(const ContactBufs& C, int i, const double* xs, double* vs) {
   const unsigned root = (unsigned)(C.zkey2[i] >> 32);
   const int m = (int)(unsigned)(C.zkey2[i] & 0xffffffffull);
   const double* rec = C.zrec + 9 * (size_t)root;
@@ -942,6 +965,11 @@ __global__ void k_riz_velocity(ContactBufs C, int n, const double* xs, double* v
   vs[3 * m + 0] = rec[3] + (-rot.x);
   vs[3 * m + 1] = rec[4] + (-rot.y);
   vs[3 * m + 2] = rec[5] + (-rot.z);
+}
+
+__global__ void k_riz_velocity(ContactBufs C, int n, const double* xs, double* vs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) riz_velocity_one(C, i, xs, vs);
 }
 
 __global__ void k_riz_labels(Arena A, int* zone_of) {
@@ -1078,13 +1106,13 @@ void sort_dedupe(const Arena& A, ContactBufs& C, int n, cudaStream_t s) {
   g_launches += 7;
 }
 
-void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, int token,
-                     cudaStream_t s) {
+void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, cudaStream_t s) {
   prof_begin(PK_IMPULSE, s);
-  k_impulse_levels<<<nblk(A.ni, 32), 32, 0, s>>>(A, C, token);
+  k_token_next<<<1, 1, 0, s>>>(A);
+  k_impulse_levels<<<nblk(A.ni, 32), 32, 0, s>>>(A, C);
   k_impulse_apply<<<A.ni, 128, 0, s>>>(A, C, ccd, xs, vs);
   prof_end(PK_IMPULSE, s);
-  g_launches += 2;
+  g_launches += 3;
 }
 
 namespace {
@@ -1155,7 +1183,7 @@ void launch_riz_add(const Arena& A, const ContactBufs& C, int nce, cudaStream_t 
 
 // rigid velocities of all zones of the active cloths; returns nothing, uses
 // C.counters[4] as the member count
-void riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, const double* v0s, cudaStream_t s) {
+int riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, const double* v0s, cudaStream_t s) {
   int* cnt = C.counters + 4;
   cudaMemsetAsync(cnt, 0, sizeof(int), s);
   k_riz_collect<<<nblk(A.nv), kT, 0, s>>>(A, C, cnt);
@@ -1163,11 +1191,12 @@ void riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, con
   int n = 0;
   cudaMemcpyAsync(&n, cnt, sizeof(int), cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
-  if (n == 0) return;
+  if (n == 0) return 0;
   cub_sort_keys(C.cub_tmp, C.cub_bytes, C.zkey, C.zkey2, n, s);
   k_riz_stats<<<nblk(n), kT, 0, s>>>(A, C, n, xs, v0s);
   k_riz_velocity<<<nblk(n), kT, 0, s>>>(C, n, xs, vs);
   g_launches += 2;
+  return n;
 }
 
 int riz_count_zones(const Arena& A, ContactBufs& C, int* zone_of, cudaStream_t s) {
@@ -1180,6 +1209,267 @@ int riz_count_zones(const Arena& A, ContactBufs& C, int* zone_of, cudaStream_t s
 void launch_riz_count(const Arena& A, cudaStream_t s) {
   k_riz_count<<<nblk(A.nv), kT, 0, s>>>(A);
   g_launches++;
+}
+
+// ---- graph frames: the pipeline with every count read on the device ---------------
+// A frame captured in a CUDA graph cannot size launches from counts the host
+// reads back.  These launchers use fixed grids and read the counts from device
+// memory; the candidate and zone sorts run at fixed, padded sizes (pad keys sort
+// last).  A count above a fixed capacity sets A.ctl->overflow, and the host then
+// re-runs the frame on the host-driven path, which grows the buffers.
+namespace {
+
+constexpr int kDevGrid = 1216;  // 8 blocks of kT threads per SM of a GB300
+
+// gates of the kernels a loop body runs only on its first or later passes
+__device__ __forceinline__ bool gate_open(const FrameCtl* c, int g) {
+  switch (g) {
+    case kGateCcdFirst: return c->ccd_pass == 0;
+    case kGateCcdLater: return c->ccd_pass > 0;
+    case kGateRizFirst: return c->riz_pass == 0;
+    case kGateRizLater: return c->riz_pass > 0;
+    default: return true;
+  }
+}
+
+__global__ void k_traverse_gated(Arena A, ContactBufs C, int gate) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < A.nt && gate_open(A.ctl, gate)) traverse_tri(A, C, t);
+}
+
+__global__ void k_traverse_dirty_gated(Arena A, ContactBufs C, int gate) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < A.nt && gate_open(A.ctl, gate)) traverse_dirty_tri(A, C, t);
+}
+
+// candidates of the previous detection without a dirty triangle (count from the device)
+__global__ void k_keep_clean_dev(Arena A, ContactBufs C, int gate) {
+  if (!gate_open(A.ctl, gate)) return;
+  const int n = min(A.ctl->last_ncand, C.cand_cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const Cand c = C.cand[i];
+    const int ta = A.node[3 * c.na + 1], tb = A.node[3 * c.nb + 1];
+    if (A.tdirty[ta] || A.tdirty[tb] || !A.active[A.tinst[ta]]) continue;
+    C.cand_sorted[atomicAdd(&C.counters[5], 1)] = c;
+  }
+}
+
+// the kept candidates to the front of C.cand; the candidate count starts there
+__global__ void k_kept_to_front(ContactBufs C) {
+  const int n = __ldcg(&C.counters[5]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) C.cand[i] = C.cand_sorted[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) C.counters[1] = n;
+}
+
+__global__ void k_mark_contacts_dev(Arena A, ContactBufs C, int gate) {
+  if (!gate_open(A.ctl, gate)) return;
+  const int n = A.ctl->last_nce;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const int* e = C.ce + 5 * c;
+    if (!A.active[A.vinst[e[1]]]) continue;
+#pragma unroll
+    for (int k = 1; k <= 4; k++) A.vdirty[e[k]] = 1;
+  }
+}
+
+__global__ void k_mark_zones_gated(Arena A, int gate) {
+  if (!gate_open(A.ctl, gate)) return;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  if (A.active[A.vinst[v]] && A.inzone[v]) A.vdirty[v] = 1;
+}
+
+// padded sort of the candidates: n = candidate count (C.counters[8])
+__global__ void k_sort_prep(Arena A, ContactBufs C, int S) {
+  const int n = C.counters[1];
+  const bool over = n > S || n > C.cand_cap;
+  C.counters[8] = over ? 0 : n;
+  C.counters[2] = 0;
+  if (over) A.ctl->overflow = 1;
+}
+
+__global__ void k_keys_lo_pad(ContactBufs C, int S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S) return;
+  C.key_a[i] = i < C.counters[8] ? key_lo(C.cand[i]) : ~0ull;
+  C.idx_a[i] = i;
+}
+
+__global__ void k_keys_hi_pad(ContactBufs C, int S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S) return;
+  C.key_a[i] = i < C.counters[8] ? key_hi(C.cand[C.idx_b[i]]) : ~0ull;
+}
+
+__global__ void k_gather_dev(ContactBufs C, int S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < S && i < C.counters[8]) C.cand_sorted[i] = C.cand[C.idx_a[i]];
+}
+
+__global__ void k_dedupe_dev(Arena A, ContactBufs C, int S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S) return;
+  const int n = C.counters[8];
+  if (i >= n) {
+    C.idx_b[i] = 0;
+    return;
+  }
+  const Cand ci = C.cand_sorted[i];
+  const bool head = (i == 0) || !same_key(C.cand_sorted[i - 1], ci);
+  C.idx_b[i] = head ? 1 : 0;
+  if (!head) return;
+  int j = i + 1;
+  bool mixed = false;
+  while (j < n && same_key(C.cand_sorted[j], ci)) {
+    mixed |= (C.cand_sorted[j].fv != ci.fv);
+    j++;
+  }
+  int win = i;
+  if (mixed)
+    for (int k = i + 1; k < j; k++)
+      if (visited_before(A, C.cand_sorted[k], C.cand_sorted[win])) win = k;
+  C.level[i] = C.cand_sorted[win].fv;
+}
+
+__global__ void k_compact_dev(ContactBufs C, int S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = C.counters[8];
+  if (i >= S || i >= n) return;
+  const int pos = C.idx_a[i];
+  if (i == n - 1) C.counters[2] = pos + C.idx_b[i];
+  if (!C.idx_b[i]) return;
+  const Cand c = C.cand_sorted[i];
+  C.ce[5 * pos + 0] = C.level[i];
+  C.ce[5 * pos + 1] = c.k[0];
+  C.ce[5 * pos + 2] = c.k[1];
+  C.ce[5 * pos + 3] = c.k[2];
+  C.ce[5 * pos + 4] = c.k[3];
+}
+
+// end of a detection: what the next incremental detection starts from, and the
+// overflow flag of the broad and narrow phases
+__global__ void k_detect_done(Arena A, ContactBufs C) {
+  FrameCtl* c = A.ctl;
+  if (C.counters[3]) c->overflow = 1;
+  c->last_ncand = C.counters[8];
+  c->last_nce = C.counters[2];
+}
+
+__global__ void k_riz_contacts_dev(Arena A, ContactBufs C) {
+  const int n = A.ctl->last_nce;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const int* e = C.ce + 5 * c;
+    if (!A.active[A.vinst[e[1]]]) continue;
+#pragma unroll
+    for (int k = 1; k <= 4; k++) A.inzone[e[k]] = 1;
+    uf_union(A.uf, e[1], e[2]);
+    uf_union(A.uf, e[1], e[3]);
+    uf_union(A.uf, e[1], e[4]);
+  }
+}
+
+// padded sort of the zone members: n = member count (C.counters[9])
+__global__ void k_zone_prep(Arena A, ContactBufs C, int S) {
+  const int n = C.counters[4];
+  const bool over = n > S;
+  if (over) A.ctl->overflow = 1;
+  C.counters[9] = over ? 0 : n;
+}
+
+__global__ void k_zone_pad(ContactBufs C, int S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < S && i >= C.counters[9]) C.zkey[i] = ~0ull;
+}
+
+__global__ void k_riz_stats_dev(Arena A, ContactBufs C, int S, const double* xs, const double* v0s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < S && i < C.counters[9]) riz_stats_one(A, C, i, C.counters[9], xs, v0s);
+}
+
+__global__ void k_riz_velocity_dev(ContactBufs C, int S, const double* xs, double* vs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < S && i < C.counters[9]) riz_velocity_one(C, i, xs, vs);
+}
+
+}  // namespace
+
+void launch_narrow_dev(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
+                       cudaStream_t s) {
+  launch_check(cudaMemsetAsync(C.counters + 6, 0, 2 * sizeof(int), s), "cudaMemsetAsync");
+  k_narrow_filter_dev<<<kDevGrid, kT, 0, s>>>(A, C, ccd, -1.0);
+  k_narrow_fv<<<kDevGrid, kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
+  k_narrow_ee<<<kDevGrid, kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
+  g_launches += 3;
+}
+
+void sort_dedupe_dev(const Arena& A, ContactBufs& C, int S, cudaStream_t s) {
+  launch_check(cudaMemsetAsync(C.ce_inst_lo, 0, sizeof(int) * (size_t)A.ni, s), "cudaMemsetAsync");
+  launch_check(cudaMemsetAsync(C.ce_inst_hi, 0, sizeof(int) * (size_t)A.ni, s), "cudaMemsetAsync");
+  k_sort_prep<<<1, 1, 0, s>>>(A, C, S);
+  k_keys_lo_pad<<<nblk(S), kT, 0, s>>>(C, S);
+  cub_sort_pairs(C.cub_tmp, C.cub_bytes, C.key_a, C.key_b, C.idx_a, C.idx_b, S, s);
+  k_keys_hi_pad<<<nblk(S), kT, 0, s>>>(C, S);
+  cub_sort_pairs(C.cub_tmp, C.cub_bytes, C.key_a, C.key_b, C.idx_b, C.idx_a, S, s);
+  k_gather_dev<<<nblk(S), kT, 0, s>>>(C, S);
+  k_dedupe_dev<<<nblk(S), kT, 0, s>>>(A, C, S);
+  cub_exclusive_sum(C.cub_tmp, C.cub_bytes, C.idx_b, C.idx_a, S, s);
+  k_compact_dev<<<nblk(S), kT, 0, s>>>(C, S);
+  k_segments<<<nblk(S), kT, 0, s>>>(A, C);
+  k_counts<<<nblk(A.ni), kT, 0, s>>>(A, C);
+  k_detect_done<<<1, 1, 0, s>>>(A, C);
+  g_launches += 10;
+}
+
+void detect_dev(const Arena& A, ContactBufs& C, int ccd, int gate_full, int gate_incr, int S, const double* xs,
+                const double* vs, cudaStream_t s) {
+  launch_refit(A, ccd, xs, vs, -1.0, s);
+  launch_check(cudaMemsetAsync(C.counters, 0, 4 * sizeof(int), s), "cudaMemsetAsync");
+  launch_check(cudaMemsetAsync(C.counters + 5, 0, sizeof(int), s), "cudaMemsetAsync");
+  if (gate_incr >= 0) {
+    k_keep_clean_dev<<<kDevGrid, kT, 0, s>>>(A, C, gate_incr);
+    k_kept_to_front<<<kDevGrid, kT, 0, s>>>(C);
+    k_traverse_dirty_gated<<<nblk(A.nt), kT, 0, s>>>(A, C, gate_incr);
+    g_launches += 3;
+  }
+  if (gate_full >= 0) {
+    k_traverse_gated<<<nblk(A.nt), kT, 0, s>>>(A, C, gate_full);
+    g_launches++;
+  }
+  launch_narrow_dev(A, C, ccd, xs, vs, s);
+  sort_dedupe_dev(A, C, S, s);
+}
+
+void mark_dirty_dev(const Arena& A, const ContactBufs& C, int gate_contacts, int gate_zones, cudaStream_t s) {
+  launch_check(cudaMemsetAsync(A.vdirty, 0, sizeof(int) * (size_t)A.nv, s), "cudaMemsetAsync");
+  if (gate_zones >= 0) {
+    k_mark_zones_gated<<<nblk(A.nv), kT, 0, s>>>(A, gate_zones);
+    g_launches++;
+  }
+  k_mark_contacts_dev<<<kDevGrid, kT, 0, s>>>(A, C, gate_contacts);
+  k_mark_tris<<<nblk(A.nt), kT, 0, s>>>(A);
+  g_launches += 2;
+}
+
+void riz_add_dev(const Arena& A, const ContactBufs& C, cudaStream_t s) {
+  k_riz_contacts_dev<<<kDevGrid, kT, 0, s>>>(A, C);
+  g_launches++;
+  if (A.ne > 0) {
+    k_riz_edges<<<nblk(A.ne), kT, 0, s>>>(A);
+    g_launches++;
+  }
+}
+
+void riz_apply_dev(const Arena& A, ContactBufs& C, int S, const double* xs, double* vs, const double* v0s,
+                   cudaStream_t s) {
+  int* cnt = C.counters + 4;
+  launch_check(cudaMemsetAsync(cnt, 0, sizeof(int), s), "cudaMemsetAsync");
+  k_riz_collect<<<nblk(A.nv), kT, 0, s>>>(A, C, cnt);
+  k_zone_prep<<<1, 1, 0, s>>>(A, C, S);
+  k_zone_pad<<<nblk(S), kT, 0, s>>>(C, S);
+  cub_sort_keys(C.cub_tmp, C.cub_bytes, C.zkey, C.zkey2, S, s);
+  k_riz_stats_dev<<<nblk(S), kT, 0, s>>>(A, C, S, xs, v0s);
+  k_riz_velocity_dev<<<nblk(S), kT, 0, s>>>(C, S, xs, vs);
+  g_launches += 5;
 }
 
 }  // namespace cs

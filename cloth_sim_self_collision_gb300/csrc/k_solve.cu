@@ -244,10 +244,11 @@ __device__ void factor_levels(const Arena& A, int inst, int limit) {
   }
 }
 
-__global__ void __launch_bounds__(kSolveThreads) k_ilu_factor(Arena A, const int* list) {
+__global__ void __launch_bounds__(kSolveThreads) k_ilu_factor(Arena A, const int* list, int masked) {
   __shared__ double sh[40];
   __shared__ int limit;
   const int inst = list[blockIdx.x];
+  if (masked && !A.active[inst]) return;
   const int v0 = A.voff[inst], v1 = A.voff[inst + 1];
   copy_matrix(A, v0, v1);
   factor_levels(A, inst, INT_MAX);
@@ -330,9 +331,11 @@ __device__ void ilu_apply(const Arena& A, int inst, double* z) {
 }
 
 // Solve_PCG (ilu_sparse.cpp:628-709) from dx = 0 with r = b
-__global__ void __launch_bounds__(kSolveThreads) k_pcg(Arena A, const int* list, double tol_in, int maxit_in) {
+__global__ void __launch_bounds__(kSolveThreads) k_pcg(Arena A, const int* list, double tol_in, int maxit_in,
+                                                       int masked) {
   __shared__ double sh[40];
   const int inst = list[blockIdx.x];
+  if (masked && !A.active[inst]) return;
   const DevParams& P = A.prm[inst];
   const double tol = tol_in >= 0 ? tol_in : P.tol;
   const int maxit = maxit_in >= 0 ? maxit_in : P.maxit;
@@ -468,9 +471,13 @@ __global__ void __launch_bounds__(kChunk) k_cg_spmv(Arena A) {
   }
 }
 
+// the iteration number: the launch's, or (it < 0, a graph frame) the device counter
+__device__ __forceinline__ int cg_iter(const Arena& A, int it) { return it >= 0 ? it : A.ctl->cycle; }
+
 // alpha = r.r / p.Ap; x += alpha p; r -= alpha Ap; chunk partials of r.r
-__global__ void __launch_bounds__(kChunk) k_cg_update(Arena A, int it) {
+__global__ void __launch_bounds__(kChunk) k_cg_update(Arena A, int it_in) {
   __shared__ double sh[40];
+  const int it = cg_iter(A, it_in);
   const int c = blockIdx.x;
   const int inst = A.chunk_inst[c];
   if (!A.active[inst] || A.st[inst].done) return;
@@ -493,7 +500,8 @@ __global__ void __launch_bounds__(kChunk) k_cg_update(Arena A, int it) {
 }
 
 // convergence test, beta and p = r + beta p
-__global__ void __launch_bounds__(kChunk) k_cg_direction(Arena A, int it, double tol_in, int maxit_in) {
+__global__ void __launch_bounds__(kChunk) k_cg_direction(Arena A, int it_in, double tol_in, int maxit_in) {
+  const int it = cg_iter(A, it_in);
   const int c = blockIdx.x;
   const int inst = A.chunk_inst[c];
   if (!A.active[inst] || A.st[inst].done) return;
@@ -573,18 +581,18 @@ __global__ void __launch_bounds__(kSolveThreads) k_ilu_solve(Arena A, int inst, 
 
 }  // namespace
 
-void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s) {
+void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s, bool masked) {
   if (n <= 0) return;
   prof_begin(PK_ILU_FACTOR, s);
-  k_ilu_factor<<<n, kSolveThreads, 0, s>>>(A, list);
+  k_ilu_factor<<<n, kSolveThreads, 0, s>>>(A, list, masked ? 1 : 0);
   prof_end(PK_ILU_FACTOR, s);
   g_launches++;
 }
 
-void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s) {
+void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s, bool masked) {
   if (n <= 0) return;
   prof_begin(PK_PCG, s);
-  k_pcg<<<n, kSolveThreads, 0, s>>>(A, list, tol, maxit);
+  k_pcg<<<n, kSolveThreads, 0, s>>>(A, list, tol, maxit, masked ? 1 : 0);
   prof_end(PK_PCG, s);
   g_launches++;
 }

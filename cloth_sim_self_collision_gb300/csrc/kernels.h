@@ -51,12 +51,14 @@ void launch_element_batch_contact(int n, const double* c, const DevParams* prm, 
                                   double* ddW, cudaStream_t s);
 
 // --- solvers (k_solve.cu) --------------------------------------------------
-// block ILU(0) of the ILU cloths in list (device array of cloth ids)
-void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s);
+// block ILU(0) of the ILU cloths in list (device array of cloth ids); masked:
+// only those with A.active set
+void launch_ilu_factor(const Arena& A, const int* list, int n, cudaStream_t s, bool masked = false);
 // PCG on A.b -> A.dx for the cloths in list (tol / maxit < 0: take the cloth's)
-void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s);
+void launch_pcg(const Arena& A, const int* list, int n, double tol, int maxit, cudaStream_t s, bool masked = false);
 // CG building blocks on all cloths with A.active set
 void launch_cg_init(const Arena& A, double tol, int maxit, cudaStream_t s);
+// it < 0: the iteration number is A.ctl->cycle (a graph frame)
 void launch_cg_iteration(const Arena& A, int it, double tol, int maxit, bool serial, cudaStream_t s);
 void launch_spmv(const Arena& A, const double* x, double* y, cudaStream_t s);
 // y = beta y + alpha A x over the rows [v0, v1) (MatVec's operation order)
@@ -95,20 +97,38 @@ void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* 
                    double delta_override, int npairs, cudaStream_t s);
 // sort + deduplicate ncand candidates into C.ce; returns via C.counters[2]
 void sort_dedupe(const Arena& A, ContactBufs& C, int ncand, cudaStream_t s);
-void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, int token,
-                     cudaStream_t s);
+// impulse sweep of the active cloths' contact lists (level stamps from A.ctl->token)
+void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, cudaStream_t s);
 void launch_riz_reset(const Arena& A, cudaStream_t s);
 // counts the in-zone vertices of each active cloth into st.riz_nodes
 void launch_riz_count(const Arena& A, cudaStream_t s);
 void launch_riz_add(const Arena& A, const ContactBufs& C, int nce, cudaStream_t s);
 // zone rigid velocities: v of zone members from snapshot v0 at positions xs
-void riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, const double* v0s, cudaStream_t s);
+// returns the number of zone members
+int riz_apply(const Arena& A, ContactBufs& C, const double* xs, double* vs, const double* v0s, cudaStream_t s);
 int riz_count_zones(const Arena& A, ContactBufs& C, int* zone_of_vertex_dev, cudaStream_t s);
 
 // geometry on batches (bvh_aabb.cpp:321-384, 598-662), 12 doubles of points per item
 void launch_distance_fv(int n, const double* pts, double* dist, double* w, cudaStream_t s);
 void launch_distance_ee(int n, const double* pts, double* dist, double* ratio, cudaStream_t s);
 void launch_coplanar_time(int n, const double* s0, const double* e0, double* t, cudaStream_t s);
+
+// ---- graph frames (k_collide.cu): counts read on the device, fixed launch sizes ----
+// gates: 0 always, 1 / 2 first / later CCD pass, 3 / 4 first / later impact-zone pass;
+// a negative gate leaves the kernel out
+enum GraphGate { kGateAlways = 0, kGateCcdFirst = 1, kGateCcdLater = 2, kGateRizFirst = 3, kGateRizLater = 4 };
+void launch_narrow_dev(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
+                       cudaStream_t s);
+// sorts and deduplicates C.counters[1] candidates at the padded size S
+void sort_dedupe_dev(const Arena& A, ContactBufs& C, int S, cudaStream_t s);
+// a detection: refit, incremental part (keep clean candidates, dirty traversal)
+// under gate_incr, full traversal under gate_full, narrow phase, sort
+void detect_dev(const Arena& A, ContactBufs& C, int ccd, int gate_full, int gate_incr, int S, const double* xs,
+                const double* vs, cudaStream_t s);
+void mark_dirty_dev(const Arena& A, const ContactBufs& C, int gate_contacts, int gate_zones, cudaStream_t s);
+void riz_add_dev(const Arena& A, const ContactBufs& C, cudaStream_t s);
+void riz_apply_dev(const Arena& A, ContactBufs& C, int S, const double* xs, double* vs, const double* v0s,
+                   cudaStream_t s);
 
 size_t cub_sort_bytes(int n);
 void cub_sort_pairs(void* tmp, size_t bytes, const unsigned long long* kin, unsigned long long* kout,

@@ -42,6 +42,8 @@ cudaEvent_t get_event() {
 }
 }  // namespace
 
+bool prof_enabled() { return g_on; }
+
 void prof_enable(bool on) { g_on = on; }
 
 void prof_begin(ProfKernel k, cudaStream_t s) {

@@ -36,6 +36,7 @@ extern const char* const kProfNames[PK_COUNT];
 void prof_begin(ProfKernel k, cudaStream_t s);
 void prof_end(ProfKernel k, cudaStream_t s);
 void prof_enable(bool on);
+bool prof_enabled();
 // resolves recorded events (synchronises them) and accumulates totals
 void prof_collect();
 void prof_reset();

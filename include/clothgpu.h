@@ -332,6 +332,26 @@ int cs_solve_cg_noalloc(const int *row_ptr, const int *col_idx, const double *vc
                         const double *b, double *x, int np, double tol, int maxit, double *conv, int *iter,
                         void *stream);
 
+/* ---- frame graph ------------------------------------------------------------------ */
+/* How cs_step runs a frame.  CS_FRAME_GRAPH (the default): one launch of a
+ * CUDA graph captured for the context's cloths, whose loops (refinement cycles
+ * or CG iterations, up to 5 CCD passes and up to 100 impact-zone passes of
+ * GetIntermidiateVelocityContactResolved, self_collision_cloth.cpp:398-455)
+ * are conditional graph nodes decided on the device; the host reads the
+ * frame's counters once at its end.  Contact buffers and sorts have fixed sizes
+ * in a graph: a frame that outgrows them is restored to its start and re-run
+ * host-driven, which grows them, and the graph is captured again.
+ * CS_FRAME_HOST: every frame host-driven (the host reads counters after each
+ * detection and solver cycle).  Both give the same frames bit for bit.  Frames
+ * run host-driven while per-kernel profiling or the contact log is on. */
+#define CS_FRAME_HOST 0
+#define CS_FRAME_GRAPH 1
+int cs_set_frame_mode(cs_ctx *ctx, int mode);
+/* Frames run as a graph and host-driven, graph captures, and graph frames that
+ * outgrew a fixed size (each then re-run host-driven); any pointer may be null. */
+int cs_frame_counts(cs_ctx *ctx, long long *graph_frames, long long *host_frames, long long *captures,
+                    long long *overflows);
+
 /* ---- contact log ------------------------------------------------------------------ */
 /* Test facility, off by default: with logging on, every contact resolution
  * (GetIntermidiateVelocityContactResolved, self_collision_cloth.cpp:355-456, in

@@ -1,0 +1,79 @@
+"""Frames captured as a CUDA graph (cs_set_frame_mode CS_FRAME_GRAPH, the
+default) against host-driven frames (CS_FRAME_HOST) on the same cloths: every
+state and every frame counter equal bit for bit, in free fall and through
+contact, for both precisions and for the ILU(0) sheet, and one host launch per
+graph frame.  A graph frame whose contact lists outgrow the graph's fixed sort
+sizes is restored and re-run host-driven, and a new graph is captured: forced
+here with small minimum sizes, with the frames still equal bit for bit."""
+import os
+
+import numpy as np
+import pytest
+
+from cloth_sim_self_collision_gb300 import scene
+
+pytestmark = pytest.mark.gpu
+
+STAT_KEYS = ("solver_iterations", "n_prx", "n_ccd", "n_ccd_passes", "n_riz_passes", "n_riz_last", "n_riz_total",
+             "riz_nodes", "impulse_applied", "ilu_singular", "diverged")
+
+
+def run(cloths, prec, graph, frames, every=10):
+    from cloth_sim_self_collision_gb300 import build
+    build.build()
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    ctx = ClothContext(0, prec)
+    try:
+        ctx.frame_mode(graph)
+        ids = [ctx.add_cloth(c) for c in cloths]
+        ctx.step(1)
+        launches0 = ctx.launch_count()
+        states, stats = [], []
+        for f in range(2, frames + 1):
+            ctx.step(1)
+            stats.append([{k: ctx.stats(i)[k] for k in STAT_KEYS} for i in ids])
+            if f % every == 0:
+                states.append([ctx.get_state(i) for i in ids])
+        return states, stats, ctx.frame_counts(), ctx.launch_count() - launches0, frames - 1
+    finally:
+        ctx.close()
+
+
+def same(a, b):
+    for sa, sb in zip(a[0], b[0]):
+        for (xa, va), (xb, vb) in zip(sa, sb):
+            if not (np.array_equal(xa, xb) and np.array_equal(va, vb)):
+                return False
+    return a[1] == b[1]
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_graph_frames_equal_host_frames(prec):
+    cl = scene.config_batch(count=16)
+    g = run(cl, prec, True, 40)
+    h = run(cl, prec, False, 40)
+    assert same(g, h)
+    assert g[2]["graph_frames"] >= g[4] - g[2]["overflows"] and h[2]["graph_frames"] == 0
+    touched = sum(s["n_prx"] > 0 for fr in g[1] for s in fr)
+    assert touched > 20, touched
+    # one graph launch per frame, plus the host-driven re-runs of frames that outgrew the graph
+    print(f"{prec}: launches per frame graph {g[3] / g[4]:.1f}, host {h[3] / h[4]:.1f}; {g[2]}")
+    assert g[3] <= g[4] + 400 * g[2]["overflows"]
+
+
+def test_graph_frames_ilu_sheet():
+    c = scene.config_small()
+    g = run([c], "fp64", True, 120)
+    h = run([c], "fp64", False, 120)
+    assert same(g, h)
+    assert g[2]["graph_frames"] > 0
+
+
+def test_graph_overflow_rerun_and_recapture(monkeypatch):
+    monkeypatch.setenv("CLOTHGPU_GRAPH_SORT_MIN", "64")
+    monkeypatch.setenv("CLOTHGPU_GRAPH_ZONE_MIN", "16")
+    cl = scene.config_batch(count=16)
+    g = run(cl, "mixed", True, 40)
+    h = run(cl, "mixed", False, 40)
+    assert same(g, h)
+    assert g[2]["overflows"] > 0 and g[2]["captures"] > 1 and g[2]["graph_frames"] > 0, g[2]
