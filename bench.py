@@ -172,6 +172,8 @@ def timed_batch(ctx, steps, warmup, stream, nv):
 
     ctx.step(warmup)
     ctx.synchronize()
+    # launch shapes timed on two frames from here (the state is restored)
+    tune = ctx.autotune(2)
     torch.cuda.synchronize()
     # the state at the start of the timed frames (the end-to-end and profiled
     # passes replay the same frames from it)
@@ -187,7 +189,7 @@ def timed_batch(ctx, steps, warmup, stream, nv):
     torch.cuda.synchronize()
     ctx.synchronize()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
-    return step_ms, ctx.launch_count() - launches0, (x0, v0)
+    return step_ms, ctx.launch_count() - launches0, (x0, v0), tune
 
 
 def profiled_replay(ctx, steps, start, profile_names=()):
@@ -447,13 +449,14 @@ def native(args):
         clocks = ClockSampler(local)
         barrier(world)
         clocks.start()
-        step_ms, launches, start = timed_batch(ctx, args.steps, args.warmup, stream, nv)
+        step_ms, launches, start, tune = timed_batch(ctx, args.steps, args.warmup, stream, nv)
         clk = clocks.stop()
         barrier(world)
         total_ms = max_over_ranks(sum(step_ms), world)
         res = {"value": world * nv * args.steps / (total_ms / 1e3), "ms_per_step": total_ms / args.steps,
                "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
-               "launches": launches, "clocks": clk, "nv": nv, "nb": nb_total, "start": start}
+               "launches": launches, "clocks": clk, "nv": nv, "nb": nb_total, "start": start, "tune": tune,
+               "frames": ctx.frame_counts()}
         if not results:
             # end to end through the C ABI, on the same frames: pinned host state
             # in, frame, state out
@@ -536,6 +539,11 @@ def native(args):
         "p50_step_ms": head["p50_step_ms"], "p99_step_ms": head["p99_step_ms"],
         "e2e": head["e2e"], "roofline": roof, "dominant_kernel": dominant,
         "gpu_launches": int(head["launches"]), "clocks": head["clocks"],
+        "frame_graph": {"frames": head["frames"],
+                        "note": "gpu_launches counts host-issued launches: one CUDA graph launch per graph "
+                                "frame (kernels inside the graph are not counted), plus the launches of "
+                                "frames re-run host-driven"},
+        "autotune": head["tune"],
         "kernel_ms": {k: [round(v[0], 3), v[1]] for k, v in prof.items() if v[1]},
         "contact_counts": head["counts"],
     }

@@ -122,6 +122,13 @@ class ClothContext:
         self._ck(self.L.cs_profile_read(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def autotune(self, frames: int = 2) -> dict:
+        """Launch shapes timed on `frames` frames from the current state (which is
+        restored); the fastest are kept and cached per arena shape."""
+        r = N.CsTuneResult()
+        self._ck(self.L.cs_autotune(self.h, frames, ctypes.byref(r)))
+        return r.as_dict()
+
     def frame_mode(self, graph: bool):
         """Frames as one captured CUDA graph each (True, the default) or host-driven."""
         self._ck(self.L.cs_set_frame_mode(self.h, 1 if graph else 0))

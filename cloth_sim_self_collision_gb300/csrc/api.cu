@@ -5,6 +5,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <tuple>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -389,8 +391,8 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
       }
       A.slice_pbytes = m.upload(pb, s);
       A.dg_range = m.alloc<unsigned>(2 * (size_t)std::max(ni, 1));
-      A.grid_bar = m.alloc<unsigned int>(4);
-      CK(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s));
+      A.grid_bar = m.alloc<unsigned int>(8);
+      CK(cudaMemsetAsync(A.grid_bar, 0, 8 * sizeof(unsigned int), s));
     }
     A.mixed = 1;
   }
@@ -525,7 +527,7 @@ void run_mixed(cs_ctx* c, const std::vector<int>& act) {
   for (int cyc = 0; cyc < maxcycles; cyc++) {
     unsigned gave_up = 0;
     if (c->mx_persistent) {
-      launch_mx_inner_persistent(A, eta, cap, c->mx_blocks_per_sm, c->mx_threads, c->stream);
+      launch_mx_inner_persistent(A, eta, cap, c->mx_blocks_per_sm, c->mx_threads, c->mx_tail_slices, c->stream);
       CK(cudaMemcpyAsync(&gave_up, A.grid_bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     } else {
       launch_mx_inner_init(A, c->stream);
@@ -984,6 +986,7 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_MX_ETA")) c->mx_eta = (float)std::atof(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_THREADS")) c->mx_threads = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_CAP")) c->mx_cap = std::atoi(e);
+  if (const char* e = std::getenv("CLOTHGPU_MX_TAIL_SLICES")) c->mx_tail_slices = std::atoi(e);
   *out = c;
   return CS_OK;
 }
@@ -1610,6 +1613,122 @@ int cs_coplanar_time(cs_ctx* c, int n, const double* s0, const double* e0, doubl
                        [&](std::vector<double*>& i, std::vector<double*>& o) {
                          launch_coplanar_time(n, i[0], i[1], o[0], c->stream);
                        });
+}
+
+namespace {
+// launch shapes chosen by cs_autotune, per arena shape and precision
+struct TuneKey {
+  int ni, nv, nslice, precision;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(ni, nv, nslice, precision) < std::tie(o.ni, o.nv, o.nslice, o.precision);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, cs_tune_result> g_tune;
+
+void apply_tune(cs_ctx* c, const cs_tune_result& r) {
+  c->mx_blocks_per_sm = r.mx_blocks_per_sm;
+  c->mx_tail_slices = r.mx_tail_slices;
+  c->graph_grid_per_sm = r.graph_grid_per_sm;
+  graph_release(c);
+}
+}  // namespace
+
+int cs_autotune(cs_ctx* c, int frames, cs_tune_result* out) {
+  return guarded(c, [&] {
+    ensure(c);
+    if (c->A.ni == 0) throw ArgError("no cloths to tune on");
+    frames = std::max(1, frames);
+    const TuneKey key{c->A.ni, c->A.nv, c->A.nslice, c->precision};
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        apply_tune(c, it->second);
+        if (out) {
+          *out = it->second;
+          out->cached = 1;
+        }
+        return;
+      }
+    }
+    // the start state, restored after every candidate: frames do not depend on
+    // these launch shapes, so tuning leaves the simulation where it was
+    const size_t n3 = 3 * (size_t)c->A.nv;
+    std::vector<double> x(n3), v(n3);
+    down(c, x.data(), c->A.x, n3);
+    down(c, v.data(), c->A.v, n3);
+    CK(cudaStreamSynchronize(c->stream));
+    const std::vector<int> dead = c->dead;
+    std::vector<cs_stats> stats;
+    for (int id : c->order) stats.push_back(c->cloths[id]->stats);
+    const std::vector<int> all(c->A.ni, 1);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int timed = 0;
+    auto restore = [&] {
+      up(c, c->A.x, x.data(), n3);
+      up(c, c->A.v, v.data(), n3);
+      CK(cudaStreamSynchronize(c->stream));
+      c->dead = dead;
+      for (size_t i = 0; i < c->order.size(); i++) c->cloths[c->order[i]]->stats = stats[i];
+    };
+    auto time_cfg = [&](const cs_tune_result& r) {
+      apply_tune(c, r);
+      restore();
+      if (c->graph_mode && graph_ok(c, live(c, all))) {  // capture is not timed
+        try {
+          graph_capture(c);
+        } catch (const CudaError&) {
+          c->graph_mode = false;  // as a graph frame would: host-driven from here on
+        }
+      }
+      CK(cudaEventRecord(e0, c->stream));
+      for (int f = 0; f < frames; f++) frame(c, all);
+      CK(cudaEventRecord(e1, c->stream));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      timed++;
+      return (double)ms / frames;
+    };
+    cs_tune_result best{};
+    best.mx_blocks_per_sm = c->mx_blocks_per_sm > 0 ? c->mx_blocks_per_sm : 6;
+    best.mx_tail_slices = c->mx_tail_slices;
+    best.graph_grid_per_sm = c->graph_grid_per_sm;
+    time_cfg(best);  // untimed warm pass: contact buffers grow to these frames' needs
+    best.frame_ms = time_cfg(best);
+    // coordinate descent over the three shapes
+    auto try_values = [&](int cs_tune_result::*field, std::initializer_list<int> values) {
+      for (int val : values) {
+        if (best.*field == val) continue;
+        cs_tune_result r = best;
+        r.*field = val;
+        const double ms = time_cfg(r);
+        if (ms < best.frame_ms) {
+          best = r;
+          best.frame_ms = ms;
+        }
+      }
+    };
+    if (c->precision == CS_PREC_MIXED) {
+      try_values(&cs_tune_result::mx_blocks_per_sm, {4, 5, 6});
+      try_values(&cs_tune_result::mx_tail_slices, {0, 608, 1216, 2432, 4864});
+    }
+    if (c->graph_mode) try_values(&cs_tune_result::graph_grid_per_sm, {4, 8, 16});
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    best.candidates = timed;
+    best.cached = 0;
+    apply_tune(c, best);
+    restore();
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      g_tune[key] = best;
+    }
+    if (out) *out = best;
+  });
 }
 
 int cs_set_frame_mode(cs_ctx* c, int mode) {

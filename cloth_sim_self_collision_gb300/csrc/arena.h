@@ -157,8 +157,10 @@ struct Arena {
   // per cloth: smallest and largest diagonal entry of the assembled matrix (as
   // the bits of positive floats) for the choice of preconditioner
   unsigned* dg_range = nullptr;
-  unsigned int* grid_bar = nullptr; // [0] arrivals, [1] generation, [2] gave up, [3] cloths still iterating
+  unsigned int* grid_bar = nullptr; // [0] arrivals, [1] generation, [2] gave up, [3] cloths still iterating,
+                                    // [4] last iteration of a launch that left for the tail launch
   FrameCtl* ctl = nullptr;          // frame control on the device
+  int dev_grid = 0;                 // blocks of the grid-stride narrow-phase kernels of a graph frame
 };
 
 // scratch for the contact pipeline (grown on demand)

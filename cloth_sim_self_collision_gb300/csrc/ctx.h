@@ -107,6 +107,11 @@ struct cs_ctx {
   bool mx_persistent = true;
   int mx_blocks_per_sm = 0;
   int mx_threads = 256;  // threads per block of the persistent solve
+  // slices still iterating below which the persistent solve continues in a
+  // smaller launch (cheaper grid barriers for the last cloths); 0: one launch
+  int mx_tail_slices = 1216;
+  // blocks per SM of the grid-stride narrow-phase kernels of a graph frame
+  int graph_grid_per_sm = 8;
   // inner FP32 solve of a refinement cycle: relative residual target and cap
   float mx_eta = 1.0e-3f;
   int mx_cap = 300;

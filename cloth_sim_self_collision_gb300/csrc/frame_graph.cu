@@ -269,7 +269,7 @@ void emit_frame(cs_ctx* c, cudaStream_t s) {
     launch_mx_warm_start(A, s);
     const cudaGraphConditionalHandle h = new_handle(s, 1);
     conditional(s, b1, h, cudaGraphCondTypeWhile, [&](cudaStream_t bs) {
-      launch_mx_inner_persistent(A, c->mx_eta, c->mx_cap, c->mx_blocks_per_sm, c->mx_threads, bs);
+      launch_mx_inner_persistent(A, c->mx_eta, c->mx_cap, c->mx_blocks_per_sm, c->mx_threads, c->mx_tail_slices, bs);
       launch_mx_refine(A, -1.0, kMaxCycles, bs);
       k_ctl_mx_cond<<<1, kCtlThreads, 0, bs>>>(A, h);
     });
@@ -361,6 +361,12 @@ void graph_capture(cs_ctx* c) {
   const long long smin = es ? std::max(1LL, std::atoll(es)) : 16384, zmin = ez ? std::max(1LL, std::atoll(ez)) : 4096;
   c->g_scand = std::min(c->C.cand_cap, pow2_at_least(std::max<long long>(2LL * c->max_ncand, smin)));
   c->g_szone = std::min(A.nv, pow2_at_least(std::max<long long>(2LL * c->max_zone, zmin)));
+  {
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    A.dev_grid = std::max(1, sms * c->graph_grid_per_sm);
+  }
   // the static solver lists of the FP64 path
   c->g_ilu.clear();
   c->g_cg_cap = 0;

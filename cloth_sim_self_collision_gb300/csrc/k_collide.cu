@@ -1219,7 +1219,8 @@ void launch_riz_count(const Arena& A, cudaStream_t s) {
 // re-runs the frame on the host-driven path, which grows the buffers.
 namespace {
 
-constexpr int kDevGrid = 1216;  // 8 blocks of kT threads per SM of a GB300
+constexpr int kDevGrid = 1216;  // 8 blocks of kT threads per SM of a GB300, unless the arena sets one
+inline int dev_grid(const Arena& A) { return A.dev_grid > 0 ? A.dev_grid : kDevGrid; }
 
 // gates of the kernels a loop body runs only on its first or later passes
 __device__ __forceinline__ bool gate_open(const FrameCtl* c, int g) {
@@ -1396,9 +1397,9 @@ __global__ void k_riz_velocity_dev(ContactBufs C, int S, const double* xs, doubl
 void launch_narrow_dev(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
                        cudaStream_t s) {
   launch_check(cudaMemsetAsync(C.counters + 6, 0, 2 * sizeof(int), s), "cudaMemsetAsync");
-  k_narrow_filter_dev<<<kDevGrid, kT, 0, s>>>(A, C, ccd, -1.0);
-  k_narrow_fv<<<kDevGrid, kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
-  k_narrow_ee<<<kDevGrid, kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
+  k_narrow_filter_dev<<<dev_grid(A), kT, 0, s>>>(A, C, ccd, -1.0);
+  k_narrow_fv<<<dev_grid(A), kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
+  k_narrow_ee<<<dev_grid(A), kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
   g_launches += 3;
 }
 
@@ -1426,8 +1427,8 @@ void detect_dev(const Arena& A, ContactBufs& C, int ccd, int gate_full, int gate
   launch_check(cudaMemsetAsync(C.counters, 0, 4 * sizeof(int), s), "cudaMemsetAsync");
   launch_check(cudaMemsetAsync(C.counters + 5, 0, sizeof(int), s), "cudaMemsetAsync");
   if (gate_incr >= 0) {
-    k_keep_clean_dev<<<kDevGrid, kT, 0, s>>>(A, C, gate_incr);
-    k_kept_to_front<<<kDevGrid, kT, 0, s>>>(C);
+    k_keep_clean_dev<<<dev_grid(A), kT, 0, s>>>(A, C, gate_incr);
+    k_kept_to_front<<<dev_grid(A), kT, 0, s>>>(C);
     k_traverse_dirty_gated<<<nblk(A.nt), kT, 0, s>>>(A, C, gate_incr);
     g_launches += 3;
   }
@@ -1445,13 +1446,13 @@ void mark_dirty_dev(const Arena& A, const ContactBufs& C, int gate_contacts, int
     k_mark_zones_gated<<<nblk(A.nv), kT, 0, s>>>(A, gate_zones);
     g_launches++;
   }
-  k_mark_contacts_dev<<<kDevGrid, kT, 0, s>>>(A, C, gate_contacts);
+  k_mark_contacts_dev<<<dev_grid(A), kT, 0, s>>>(A, C, gate_contacts);
   k_mark_tris<<<nblk(A.nt), kT, 0, s>>>(A);
   g_launches += 2;
 }
 
 void riz_add_dev(const Arena& A, const ContactBufs& C, cudaStream_t s) {
-  k_riz_contacts_dev<<<kDevGrid, kT, 0, s>>>(A, C);
+  k_riz_contacts_dev<<<dev_grid(A), kT, 0, s>>>(A, C);
   g_launches++;
   if (A.ne > 0) {
     k_riz_edges<<<nblk(A.ne), kT, 0, s>>>(A);

@@ -445,7 +445,8 @@ __device__ __forceinline__ bool portion(const Arena& A, const PersistRange& R, b
 }
 
 template <int kPersistThreads>
-__global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads) k_mx_persist(Arena A, float eta, int cap) {
+__global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads)
+    k_mx_persist(Arena A, float eta, int cap, int exit_slices, int resume) {
   constexpr int kPersistWarps = kPersistThreads / 32;
   __shared__ double sh[kPersistWarps];
   __shared__ int s_wsum[kPersistWarps];
@@ -464,12 +465,21 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads) k_mx_
   if (threadIdx.x == 0) s_left = ((volatile unsigned*)A.grid_bar)[3];
   __syncthreads();
   unsigned cut_at = 0xffffffffu;  // cloths iterating when the range was cut
-  for (int it = 1; it <= cap; it++) {
+  // a resumed launch continues after the last iteration the first one ran
+  const int it0 = resume ? (int)((volatile unsigned*)A.grid_bar)[4] + 1 : 1;
+  for (int it = it0; it <= cap; it++) {
     const unsigned left = (unsigned)s_left;
     if (left == 0u) break;
     if (compact && left != cut_at) {
       compact_range<kPersistThreads>(A, s_pref, s_wsum, R);
       cut_at = left;
+    }
+    // fewer slices left than exit_slices: every block leaves here (they all
+    // read the same cut), and a launch with fewer blocks, whose grid barriers
+    // cost less, resumes at this iteration
+    if (exit_slices > 0 && compact && s_pref[A.ni] < exit_slices) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) A.grid_bar[4] = (unsigned)(it - 1);
+      break;
     }
     // iteration 1 reads r_1, w_1 from r32, w32 (the start kernels) and no s, p
     const bool odd = (it & 1) != 0;
@@ -802,7 +812,7 @@ void launch_mx_inner_iteration(const Arena& A, int it, float eta, int cap, cudaS
 }
 
 template <int T>
-static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm, cudaStream_t s) {
+static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm, int tail_slices, cudaStream_t s) {
   int dev = 0, sms = 0, occ = 0;
   launch_check(cudaGetDevice(&dev), "cudaGetDevice");
   launch_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
@@ -811,17 +821,30 @@ static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm
   if (blocks_per_sm > 0) occ = std::min(occ, blocks_per_sm);
   // at least one slice per warp
   const int grid = std::max(1, std::min((A.nslice + T / 32 - 1) / (T / 32), sms * std::max(occ, 1)));
-  void* args[] = {(void*)&A, (void*)&eta, (void*)&cap};
+  // the tail launch: one warp for each of at most tail_slices slices
+  const bool tail = tail_slices > 0 && A.ni <= kRebalanceMax;
+  const int grid2 = std::max(1, std::min(grid, (tail_slices + T / 32 - 1) / (T / 32)));
+  int exit1 = tail && grid2 < grid ? tail_slices : 0, resume = 0;
+  void* args[] = {(void*)&A, (void*)&eta, (void*)&cap, (void*)&exit1, (void*)&resume};
   prof_begin(PK_MX_PERSIST, s);
   launch_check(cudaLaunchCooperativeKernel((const void*)k_mx_persist<T>, dim3(grid), dim3(T), args, 0, s),
                "cudaLaunchCooperativeKernel");
   prof_end(PK_MX_PERSIST, s);
   g_launches += 1;
+  if (exit1 > 0) {
+    int exit2 = 0, resume2 = 1;
+    void* args2[] = {(void*)&A, (void*)&eta, (void*)&cap, (void*)&exit2, (void*)&resume2};
+    prof_begin(PK_MX_PERSIST, s);
+    launch_check(cudaLaunchCooperativeKernel((const void*)k_mx_persist<T>, dim3(grid2), dim3(T), args2, 0, s),
+                 "cudaLaunchCooperativeKernel");
+    prof_end(PK_MX_PERSIST, s);
+    g_launches += 1;
+  }
 }
 
-void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, int threads,
+void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, int threads, int tail_slices,
                                 cudaStream_t s) {
-  launch_check(cudaMemsetAsync(A.grid_bar, 0, 4 * sizeof(unsigned int), s), "cudaMemsetAsync");
+  launch_check(cudaMemsetAsync(A.grid_bar, 0, 8 * sizeof(unsigned int), s), "cudaMemsetAsync");
   launch_check(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(A.ni, 1), s), "cudaMemsetAsync");
   const int blocks = (A.nslice * 32 + kSliceThreads - 1) / kSliceThreads;
   k_mx_inner_init<<<blocks, kSliceThreads, 0, s>>>(A);
@@ -829,11 +852,11 @@ void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_p
   k_mx_pstart<<<(A.ni * 32 + 127) / 128, 128, 0, s>>>(A);
   g_launches += 3;
   if (threads == 1024)
-    persist_launch<1024>(A, eta, cap, blocks_per_sm, s);
+    persist_launch<1024>(A, eta, cap, blocks_per_sm, tail_slices, s);
   else if (threads == 512)
-    persist_launch<512>(A, eta, cap, blocks_per_sm, s);
+    persist_launch<512>(A, eta, cap, blocks_per_sm, tail_slices, s);
   else
-    persist_launch<256>(A, eta, cap, blocks_per_sm, s);
+    persist_launch<256>(A, eta, cap, blocks_per_sm, tail_slices, s);
 }
 
 void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s) {

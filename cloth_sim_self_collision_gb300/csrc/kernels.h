@@ -75,8 +75,10 @@ void launch_mx_warm_start(const Arena& A, cudaStream_t s);
 void launch_mx_inner_iteration(const Arena& A, int it, float eta, int cap, cudaStream_t s);
 // the whole inner FP32 CG of one refinement cycle (up to cap iterations) in one
 // cooperative launch; blocks_per_sm <= 0 picks the occupancy limit
-// threads per block: 256, 512 or 1024
-void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, int threads,
+// threads per block: 256, 512 or 1024; tail_slices > 0: once fewer slices
+// than that are still iterating, a second launch with one warp per slice
+// finishes the solve (0: one launch)
+void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, int threads, int tail_slices,
                                 cudaStream_t s);
 void launch_mx_refine(const Arena& A, double tol, int maxcycles, cudaStream_t s);
 

@@ -352,6 +352,25 @@ int cs_set_frame_mode(cs_ctx *ctx, int mode);
 int cs_frame_counts(cs_ctx *ctx, long long *graph_frames, long long *host_frames, long long *captures,
                     long long *overflows);
 
+/* ---- autotuning of launch shapes ----------------------------------------------------- */
+/* No counterpart in the reference.  Times `frames` frames from the current state
+ * for candidate launch shapes (coordinate descent over the persistent solver's
+ * blocks per SM, the slice count below which it continues in a smaller tail
+ * launch, and the blocks per SM of the narrow-phase kernels of graph frames),
+ * restoring the state after each, and keeps the fastest.  The frames do not
+ * depend on these shapes, so the simulation continues exactly where it was.
+ * Results are cached per arena shape (cloths, vertices, slices, precision) for
+ * the life of the process: a later call on the same shape only applies them. */
+typedef struct cs_tune_result {
+  int mx_blocks_per_sm;   /* persistent solver: blocks of 256 threads per SM    */
+  int mx_tail_slices;     /* persistent solver: tail launch threshold (0: none)  */
+  int graph_grid_per_sm;  /* graph frames: narrow-phase blocks per SM           */
+  double frame_ms;        /* measured time of a frame with these shapes         */
+  int candidates;         /* configurations timed                               */
+  int cached;             /* 1: taken from an earlier call on the same shape    */
+} cs_tune_result;
+int cs_autotune(cs_ctx *ctx, int frames, cs_tune_result *out);
+
 /* ---- contact log ------------------------------------------------------------------ */
 /* Test facility, off by default: with logging on, every contact resolution
  * (GetIntermidiateVelocityContactResolved, self_collision_cloth.cpp:355-456, in

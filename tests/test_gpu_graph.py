@@ -56,9 +56,12 @@ def test_graph_frames_equal_host_frames(prec):
     assert g[2]["graph_frames"] >= g[4] - g[2]["overflows"] and h[2]["graph_frames"] == 0
     touched = sum(s["n_prx"] > 0 for fr in g[1] for s in fr)
     assert touched > 20, touched
-    # one graph launch per frame, plus the host-driven re-runs of frames that outgrew the graph
-    print(f"{prec}: launches per frame graph {g[3] / g[4]:.1f}, host {h[3] / h[4]:.1f}; {g[2]}")
-    assert g[3] <= g[4] + 400 * g[2]["overflows"]
+    # one graph launch per graph frame; only the frames that outgrew the graph's
+    # fixed sizes (re-run host-driven) issue kernel launches from the host
+    print(f"{prec}: host launches per frame graph {g[3] / g[4]:.1f}, host-driven {h[3] / h[4]:.1f}; {g[2]}")
+    assert g[3] * 5 < h[3]
+    if g[2]["overflows"] == 0:
+        assert g[3] == g[4]
 
 
 def test_graph_frames_ilu_sheet():
@@ -77,3 +80,34 @@ def test_graph_overflow_rerun_and_recapture(monkeypatch):
     h = run(cl, "mixed", False, 40)
     assert same(g, h)
     assert g[2]["overflows"] > 0 and g[2]["captures"] > 1 and g[2]["graph_frames"] > 0, g[2]
+
+
+def test_autotune_leaves_frames_unchanged():
+    """cs_autotune times candidate launch shapes on frames from the current state
+    and restores it: the frames that follow equal those of an untuned context
+    bit for bit, and a second context of the same shape takes the cached result."""
+    from cloth_sim_self_collision_gb300 import build
+    build.build()
+    from cloth_sim_self_collision_gb300.context import ClothContext
+    cl = scene.config_batch(count=12)
+    out = []
+    tunes = []
+    for tune in (True, False, True):
+        ctx = ClothContext(0, "mixed")
+        try:
+            ids = [ctx.add_cloth(c) for c in cl]
+            ctx.step(28)
+            if tune:
+                tunes.append(ctx.autotune(2))
+            ctx.step(4)
+            out.append([ctx.get_state(i) for i in ids])
+        finally:
+            ctx.close()
+    for a, b in ((out[0], out[1]), (out[2], out[1])):
+        for (xa, va), (xb, vb) in zip(a, b):
+            assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    t0, t1 = tunes
+    print("autotune:", t0, t1)
+    assert t0["cached"] == 0 and t0["candidates"] >= 3 and t0["frame_ms"] > 0
+    assert t1["cached"] == 1 and t1["mx_blocks_per_sm"] == t0["mx_blocks_per_sm"]
+    assert t0["mx_blocks_per_sm"] in (4, 5, 6) and t0["graph_grid_per_sm"] in (4, 8, 16)
