@@ -289,7 +289,8 @@ def small_config(device: int, frames: int = 300) -> dict:
             "cpu_port_1core": {"value": c.np * frames / cs, "ms_per_step": 1e3 * cs / frames}}
 
 
-def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, plain_budget_s: float = 40.0) -> dict:
+def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, plain_budget_s: float = 40.0,
+            plain: bool = True) -> dict:
     """The serving workload: scenes of log-uniform size (1e2..1e5 vertices) arriving
     as a Poisson process, each run for `steps` frames by the native server (one
     arena, continuous batching, admission by a 150 GB device-byte budget).
@@ -325,6 +326,20 @@ def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, pl
     done = [(c, i) for c, i in infos]
     span = max(i["t_done"] for _, i in done) - min(i["t_submit"] for _, i in done) if done else float("nan")
     vsteps = sum(c.np * steps for c, _ in done)
+    out = {
+        "workload": f"{scenes} scenes, vertex count log-uniform 1e2..1e5 (square grids), Poisson arrivals at "
+                    f"{rate}/s, {steps} frames each, 150 GB admission budget, mixed precision",
+        "rate_per_s": rate,
+        "vertex_steps_per_s": vsteps / span if done else None, "completed": len(done), "diverged": diverged,
+        "p50_step_ms": st["step_ms_p50"], "p99_step_ms": st["step_ms_p99"], "max_step_ms": st["step_ms_max"],
+        "admit_ms_p50": st["admit_ms_p50"], "admit_ms_p99": st["admit_ms_p99"],
+        "p50_request_s": float(np.percentile([i["t_done"] - i["t_submit"] for _, i in done], 50)) if done else None,
+        "p99_request_s": float(np.percentile([i["t_done"] - i["t_submit"] for _, i in done], 99)) if done else None,
+        "frames": st["frames"], "arena_swaps": st["rebuilds"], "build_ms_total": st["build_ms_total"],
+        "swap_ms_total": st["install_ms_total"], "peak_bytes": st["peak_bytes"],
+    }
+    if not plain:
+        return out
     # the plain FP64 path, one scene per context, on a sample of the same scenes
     ctx = ClothContext(device, "fp64")
     stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
@@ -347,21 +362,10 @@ def serving(device: int, scenes: int, rate: float, steps: int, seed: int = 1, pl
         if pms / 1e3 > plain_budget_s:
             break
     ctx.close()
-    out = {
-        "workload": f"{scenes} scenes, vertex count log-uniform 1e2..1e5 (square grids), Poisson arrivals at "
-                    f"{rate}/s, {steps} frames each, 150 GB admission budget, mixed precision",
-        "vertex_steps_per_s": vsteps / span if done else None, "completed": len(done), "diverged": diverged,
-        "p50_step_ms": st["step_ms_p50"], "p99_step_ms": st["step_ms_p99"], "max_step_ms": st["step_ms_max"],
-        "admit_ms_p50": st["admit_ms_p50"], "admit_ms_p99": st["admit_ms_p99"],
-        "p50_request_s": float(np.percentile([i["t_done"] - i["t_submit"] for _, i in done], 50)) if done else None,
-        "p99_request_s": float(np.percentile([i["t_done"] - i["t_submit"] for _, i in done], 99)) if done else None,
-        "frames": st["frames"], "arena_swaps": st["rebuilds"], "build_ms_total": st["build_ms_total"],
-        "swap_ms_total": st["install_ms_total"], "peak_bytes": st["peak_bytes"],
-        "plain_gpu_fp64_one_per_launch": {
-            "value": pv / (pms / 1e3) if pms > 0 else None, "unit": UNIT,
-            "sample": f"first {tried} scenes in arrival order ({used} that did not blow up), each alone in its "
-                      f"own arena for its {steps} frames"},
-    }
+    out["plain_gpu_fp64_one_per_launch"] = {
+        "value": pv / (pms / 1e3) if pms > 0 else None, "unit": UNIT,
+        "sample": f"first {tried} scenes in arrival order ({used} that did not blow up), each alone in its "
+                  f"own arena for its {steps} frames"}
     if out["vertex_steps_per_s"] and out["plain_gpu_fp64_one_per_launch"]["value"]:
         out["vs_plain_gpu"] = out["vertex_steps_per_s"] / out["plain_gpu_fp64_one_per_launch"]["value"]
     return out
@@ -562,6 +566,17 @@ def native(args):
         line["single_cloth"] = single_cloths(local)
     if not args.no_serve:
         line["serving"] = serving(local, args.serve_scenes, args.serve_rate, args.serve_steps)
+        if args.serve_rates:
+            # the latency / throughput curve over the arrival rate (the plain path
+            # is the one measured above: the same scenes in the same order)
+            pl = line["serving"]["plain_gpu_fp64_one_per_launch"]["value"]
+            sweep = []
+            for r in (float(t) for t in args.serve_rates.split(",")):
+                row = serving(local, args.serve_scenes, r, args.serve_steps, plain=False)
+                if row["vertex_steps_per_s"] and pl:
+                    row["vs_plain_gpu"] = row["vertex_steps_per_s"] / pl
+                sweep.append(row)
+            line["serving_sweep"] = sweep
     if not args.no_cpu:
         line["cpu_baseline"] = run_cpu_baseline(cloths)
     print(json.dumps(line), flush=True)
@@ -661,6 +676,8 @@ def main():
     ap.add_argument("--serve-scenes", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, scenes per second")
     ap.add_argument("--serve-steps", type=int, default=200)
+    ap.add_argument("--serve-rates", default="",
+                    help="comma-separated Poisson arrival rates for a latency / throughput sweep of the server")
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
         raise SystemExit("need --steps >= 1 and --warmup >= 0")

@@ -28,13 +28,15 @@ def run(cloths, prec, graph, frames, every=10):
         ids = [ctx.add_cloth(c) for c in cloths]
         ctx.step(1)
         launches0 = ctx.launch_count()
-        states, stats = [], []
+        states, stats, per_frame = [], [], []
         for f in range(2, frames + 1):
+            l0 = ctx.launch_count()
             ctx.step(1)
+            per_frame.append(ctx.launch_count() - l0)
             stats.append([{k: ctx.stats(i)[k] for k in STAT_KEYS} for i in ids])
             if f % every == 0:
                 states.append([ctx.get_state(i) for i in ids])
-        return states, stats, ctx.frame_counts(), ctx.launch_count() - launches0, frames - 1
+        return states, stats, ctx.frame_counts(), ctx.launch_count() - launches0, frames - 1, per_frame
     finally:
         ctx.close()
 
@@ -59,9 +61,9 @@ def test_graph_frames_equal_host_frames(prec):
     # one graph launch per graph frame; only the frames that outgrew the graph's
     # fixed sizes (re-run host-driven) issue kernel launches from the host
     print(f"{prec}: host launches per frame graph {g[3] / g[4]:.1f}, host-driven {h[3] / h[4]:.1f}; {g[2]}")
-    assert g[3] * 5 < h[3]
-    if g[2]["overflows"] == 0:
-        assert g[3] == g[4]
+    # (frames before the first capture count as graph frames once captured)
+    assert g[3] <= g[4] + g[2]["overflows"] * max(h[5])
+    assert sum(n == 1 for n in g[5]) >= g[4] - g[2]["overflows"] - 1
 
 
 def test_graph_frames_ilu_sheet():
