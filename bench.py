@@ -164,7 +164,7 @@ def run_cpu_baseline(cloths, budget_s: float = 12.0) -> dict:
 
 
 # --------------------------------------------------------------------------------------
-def timed_batch(ctx, steps, warmup, stream, nv):
+def timed_batch(ctx, steps, warmup, stream, nv, tune_frames=2, profile_window=False):
     """W untimed frames, then K frames of every cloth in the context timed with
     per-frame CUDA events on the library's stream (no per-kernel profiling).
     Returns (per-frame ms list, launches, start state of the timed frames)."""
@@ -173,7 +173,7 @@ def timed_batch(ctx, steps, warmup, stream, nv):
     ctx.step(warmup)
     ctx.synchronize()
     # launch shapes timed on two frames from here (the state is restored)
-    tune = ctx.autotune(2)
+    tune = ctx.autotune(tune_frames) if tune_frames else None
     torch.cuda.synchronize()
     # the state at the start of the timed frames (the end-to-end and profiled
     # passes replay the same frames from it)
@@ -182,12 +182,16 @@ def timed_batch(ctx, steps, warmup, stream, nv):
     ctx.get_states(x0, v0)
     launches0 = ctx.launch_count()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    if profile_window:
+        torch.cuda.cudart().cudaProfilerStart()
     ev[0].record(stream)
     for k in range(steps):
         ctx.step(1)
         ev[k + 1].record(stream)
     torch.cuda.synchronize()
     ctx.synchronize()
+    if profile_window:
+        torch.cuda.cudart().cudaProfilerStop()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
     return step_ms, ctx.launch_count() - launches0, (x0, v0), tune
 
@@ -212,10 +216,10 @@ def profiled_replay(ctx, steps, start, profile_names=()):
 
 PROFILED = ("cg_spmv", "cg_update", "cg_direction", "tri_elements", "slot_reduce", "rhs", "refit", "traverse",
             "narrow", "impulse", "pcg", "ilu_factor", "mx_spmv", "mx_update", "mx_direction", "mx_residual",
-            "mx_persist", "narrow_filter", "narrow_fv", "narrow_ee", "sort")
+            "mx_persist", "narrow_filter", "narrow_fv", "narrow_ee", "narrow_ccd64", "sort")
 
 
-NESTED = ("narrow_filter", "narrow_fv", "narrow_ee")
+NESTED = ("narrow_filter", "narrow_fv", "narrow_ee", "narrow_ccd64")
 
 
 def plain_one_per_launch(cloths, device, steps: int, warmup: int, start, budget_s: float = 8.0) -> dict:
@@ -446,6 +450,7 @@ def native(args):
     results = {}
     for prec in (["mixed", "fp64"] if args.precision == "both" else [args.precision]):
         ctx = ClothContext(local, prec)
+        ctx.frame_mode(args.frame_mode == "graph")
         ids = [ctx.add_cloth(c) for c in cloths]
         nv = ctx.num_vertices()
         nb_total = sum(int(ctx.pattern(i)[0][-1]) for i in ids)
@@ -453,7 +458,8 @@ def native(args):
         clocks = ClockSampler(local)
         barrier(world)
         clocks.start()
-        step_ms, launches, start, tune = timed_batch(ctx, args.steps, args.warmup, stream, nv)
+        step_ms, launches, start, tune = timed_batch(ctx, args.steps, args.warmup, stream, nv,
+                                                     0 if args.no_tune else 2, args.profile_window)
         clk = clocks.stop()
         barrier(world)
         total_ms = max_over_ranks(sum(step_ms), world)
@@ -673,6 +679,12 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving workload")
     ap.add_argument("--no-single", action="store_true", help="skip the single-cloth configurations")
     ap.add_argument("--no-small", action="store_true", help="skip the 21x21 ILU(0)-PCG sheet")
+    ap.add_argument("--frame-mode", default="graph", choices=["graph", "host"],
+                    help="frames as one captured CUDA graph each (default) or host-driven (profilers that "
+                         "cannot see into conditional graph nodes)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotuning)")
+    ap.add_argument("--profile-window", action="store_true",
+                    help="cudaProfilerStart/Stop around the timed frames (ncu --profile-from-start off)")
     ap.add_argument("--serve-scenes", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, scenes per second")
     ap.add_argument("--serve-steps", type=int, default=200)

@@ -42,13 +42,14 @@ EXPORTS = [
     "cs_server_get_stats", "cs_server_last_error", "cs_server_destroy", "cs_scene_device_bytes",
     "cs_vertex_normals", "cs_contact_log", "cs_contact_log_read", "cs_matvec", "cs_set_matrix", "cs_ilu_solve",
     "cs_distance_fv", "cs_distance_ee", "cs_coplanar_time", "cs_last_residual", "cs_set_frame_mode",
-    "cs_frame_counts", "cs_autotune",
+    "cs_frame_counts", "cs_frame_overflows", "cs_autotune",
 ]
 
 
 class CsTuneResult(ctypes.Structure):
     _fields_ = [("mx_blocks_per_sm", ctypes.c_int), ("mx_tail_slices", ctypes.c_int),
-                ("graph_grid_per_sm", ctypes.c_int), ("frame_ms", ctypes.c_double), ("candidates", ctypes.c_int),
+                ("graph_grid_per_sm", ctypes.c_int), ("narrow_regs", ctypes.c_int), ("frame_ms", ctypes.c_double),
+                ("candidates", ctypes.c_int),
                 ("cached", ctypes.c_int)]
 
     def as_dict(self) -> dict:
@@ -218,6 +219,7 @@ def load(path: str | None = None, build_if_missing: bool = False):
     f("cs_autotune", i, _V, i, ctypes.POINTER(CsTuneResult))
     LL = ctypes.POINTER(ctypes.c_longlong)
     f("cs_frame_counts", i, _V, LL, LL, LL, LL)
+    f("cs_frame_overflows", i, _V, LL)
     f("cs_matvec", i, _V, i, d, _D, d, _D)
     f("cs_last_residual", i, _V, i, _D)
     f("cs_set_matrix", i, _V, i, _D, _D)

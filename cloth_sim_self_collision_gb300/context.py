@@ -137,7 +137,11 @@ class ClothContext:
         """Graph frames, host-driven frames, graph captures, graph frames re-run host-driven."""
         v = [ctypes.c_longlong() for _ in range(4)]
         self._ck(self.L.cs_frame_counts(self.h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("graph_frames", "host_frames", "captures", "overflows"), (x.value for x in v)))
+        d = dict(zip(("graph_frames", "host_frames", "captures", "overflows"), (x.value for x in v)))
+        r = (ctypes.c_longlong * 4)()
+        self._ck(self.L.cs_frame_overflows(self.h, r))
+        d["overflow_reasons"] = dict(zip(("sort", "zone", "buffers", "solver"), r))
+        return d
 
     def log_contacts(self, enable: bool = True):
         """Record, per detection of each cloth's next contact resolution, (kind,

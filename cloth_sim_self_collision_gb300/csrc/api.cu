@@ -49,6 +49,8 @@ void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t
   C.q_cap[1] = q_ee > 0 ? q_ee : (int)std::min<long long>(2LL * pair_cap, 0x7fffffffLL);
   C.queue[0] = m.alloc<int2>(C.q_cap[0]);
   C.queue[1] = m.alloc<int2>(C.q_cap[1]);
+  C.queue64[0] = m.alloc<int2>(C.q_cap[0]);
+  C.queue64[1] = m.alloc<int2>(C.q_cap[1]);
   C.cand = m.alloc<Cand>(cand_cap);
   C.cand_sorted = m.alloc<Cand>(cand_cap);
   C.key_a = m.alloc<unsigned long long>(cand_cap);
@@ -407,6 +409,7 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
 // Makes o the context's arena; the previous arena's buffers end up in o.
 void install(cs_ctx* c, ArenaSet& o) {
   graph_release(c);
+  o.A.narrow_regs = c->narrow_regs;
   std::swap(c->A, o.A);
   std::swap(c->C, o.C);
   std::swap(c->mem, o.mem);
@@ -987,6 +990,8 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_MX_THREADS")) c->mx_threads = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_CAP")) c->mx_cap = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_TAIL_SLICES")) c->mx_tail_slices = std::atoi(e);
+  if (const char* e = std::getenv("CLOTHGPU_NARROW_REGS")) c->narrow_regs = std::atoi(e) == 128 ? 128 : 0;
+  c->A.narrow_regs = c->narrow_regs;
   *out = c;
   return CS_OK;
 }
@@ -1630,6 +1635,8 @@ void apply_tune(cs_ctx* c, const cs_tune_result& r) {
   c->mx_blocks_per_sm = r.mx_blocks_per_sm;
   c->mx_tail_slices = r.mx_tail_slices;
   c->graph_grid_per_sm = r.graph_grid_per_sm;
+  c->narrow_regs = r.narrow_regs;
+  c->A.narrow_regs = r.narrow_regs;
   graph_release(c);
 }
 }  // namespace
@@ -1697,6 +1704,7 @@ int cs_autotune(cs_ctx* c, int frames, cs_tune_result* out) {
     best.mx_blocks_per_sm = c->mx_blocks_per_sm > 0 ? c->mx_blocks_per_sm : 6;
     best.mx_tail_slices = c->mx_tail_slices;
     best.graph_grid_per_sm = c->graph_grid_per_sm;
+    best.narrow_regs = c->narrow_regs;
     time_cfg(best);  // untimed warm pass: contact buffers grow to these frames' needs
     best.frame_ms = time_cfg(best);
     // coordinate descent over the three shapes
@@ -1717,6 +1725,7 @@ int cs_autotune(cs_ctx* c, int frames, cs_tune_result* out) {
       try_values(&cs_tune_result::mx_tail_slices, {0, 608, 1216, 2432, 4864});
     }
     if (c->graph_mode) try_values(&cs_tune_result::graph_grid_per_sm, {4, 8, 16});
+    try_values(&cs_tune_result::narrow_regs, {0, 128});
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     best.candidates = timed;
@@ -1746,6 +1755,13 @@ int cs_frame_counts(cs_ctx* c, long long* graph_frames, long long* host_frames, 
     if (host_frames) *host_frames = c->host_frames;
     if (captures) *captures = c->g_captures;
     if (overflows) *overflows = c->g_overflows;
+  });
+}
+
+int cs_frame_overflows(cs_ctx* c, long long* reasons) {
+  if (!reasons) return CS_ERR_ARG;
+  return guarded(c, [&] {
+    for (int k = 0; k < 4; k++) reasons[k] = c->g_over_reason[k];
   });
 }
 

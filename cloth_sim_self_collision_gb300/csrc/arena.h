@@ -70,11 +70,17 @@ struct InstState {
 // GetIntermidiateVelocityContactResolved (self_collision_cloth.cpp:398-455:
 // up to 5 CCD passes, up to 100 impact-zone passes) and of the solvers run as
 // conditional graph nodes whose conditions kernels set from these counters.
+// reasons a graph frame is re-run host-driven (FrameCtl::overflow bits)
+constexpr int kOverflowSort = 1;     // candidates beyond the padded sort size
+constexpr int kOverflowZone = 2;     // impact-zone members beyond the padded sort size
+constexpr int kOverflowBuffers = 4;  // leaf pairs, test queues or candidates beyond their buffers
+constexpr int kOverflowSolver = 8;   // refinement cycles beyond the graph's cap, or a barrier gave up
+
 struct FrameCtl {
   int ccd_pass;     // CCD passes run in this frame
   int riz_pass;     // impact-zone passes run
   int cycle;        // refinement cycles (mixed) / CG iterations (FP64)
-  int overflow;     // a fixed-size buffer overflowed (the host re-runs the frame)
+  int overflow;     // a fixed size was outgrown (the host re-runs the frame): bits kOverflow*
   int last_ncand;   // candidates of the last detection (kept for the incremental one)
   int last_nce;     // contacts of the last detection
   int token;        // stamp of the impulse level schedule (host and graph frames share it)
@@ -161,6 +167,7 @@ struct Arena {
                                     // [4] last iteration of a launch that left for the tail launch
   FrameCtl* ctl = nullptr;          // frame control on the device
   int dev_grid = 0;                 // blocks of the grid-stride narrow-phase kernels of a graph frame
+  int narrow_regs = 0;              // 128: FP64 narrow-phase kernels capped at 128 registers
 };
 
 // scratch for the contact pipeline (grown on demand)
@@ -171,6 +178,9 @@ struct ContactBufs {
   // test, as (pair index, test index): face-vertex [0] and edge-edge [1]
   int q_cap[2] = {0, 0};
   int2* queue[2] = {nullptr, nullptr};
+  // continuous-collision tests the FP32 certificates left to the FP64 test
+  // (face-vertex, edge-edge; counts in counters[10], counters[11])
+  int2* queue64[2] = {nullptr, nullptr};
   Cand* cand = nullptr;
   Cand* cand_sorted = nullptr;
   unsigned long long *key_a = nullptr, *key_b = nullptr;

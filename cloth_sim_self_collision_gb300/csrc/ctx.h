@@ -112,6 +112,8 @@ struct cs_ctx {
   int mx_tail_slices = 1216;
   // blocks per SM of the grid-stride narrow-phase kernels of a graph frame
   int graph_grid_per_sm = 8;
+  // register variant of the FP64 narrow-phase kernels (0 free, 128 capped)
+  int narrow_regs = 0;
   // inner FP32 solve of a refinement cycle: relative residual target and cap
   float mx_eta = 1.0e-3f;
   int mx_cap = 300;
@@ -141,6 +143,7 @@ struct cs_ctx {
   double* gsave = nullptr;
   size_t gsave_n = 0;
   long long g_frames = 0, g_captures = 0, g_overflows = 0, host_frames = 0;
+  long long g_over_reason[4] = {0, 0, 0, 0};  // overflows by reason: sort, zone, buffers, solver
 };
 
 namespace cs {

@@ -162,7 +162,7 @@ __global__ void k_ctl_mx_cond(Arena A, cudaGraphConditionalHandle h) {
     FrameCtl* c = A.ctl;
     const int cyc = ++c->cycle;
     const bool gave_up = ((volatile unsigned*)A.grid_bar)[2] != 0u;
-    if (gave_up) c->overflow = 1;
+    if (gave_up) c->overflow |= kOverflowSolver;
     cudaGraphSetConditional(h, cyc < kMaxCycles && any && !gave_up ? 1u : 0u);
   }
 }
@@ -353,14 +353,18 @@ void graph_capture(cs_ctx* c) {
   Arena& A = c->A;
   for (int k = 0; k < 2; k++)
     if (!c->gstream[k]) CK(cudaStreamCreateWithFlags(&c->gstream[k], cudaStreamNonBlocking));
-  // padded sort sizes from the counts the host-driven frames saw (at least
-  // CLOTHGPU_GRAPH_SORT_MIN candidates and CLOTHGPU_GRAPH_ZONE_MIN zone members;
-  // tests lower them to make graph frames outgrow their sizes)
+  // padded sort sizes: four times the largest counts the frames so far saw
+  // (contacts grow as cloths settle into contact, and a frame that outgrows
+  // the graph costs a graph frame, a host-driven frame and a capture, far more
+  // than sorting padded keys), at least CLOTHGPU_GRAPH_SORT_MIN candidates and
+  // CLOTHGPU_GRAPH_ZONE_MIN zone members (tests lower them to make graph
+  // frames outgrow their sizes)
   const char* es = std::getenv("CLOTHGPU_GRAPH_SORT_MIN");
   const char* ez = std::getenv("CLOTHGPU_GRAPH_ZONE_MIN");
-  const long long smin = es ? std::max(1LL, std::atoll(es)) : 16384, zmin = ez ? std::max(1LL, std::atoll(ez)) : 4096;
-  c->g_scand = std::min(c->C.cand_cap, pow2_at_least(std::max<long long>(2LL * c->max_ncand, smin)));
-  c->g_szone = std::min(A.nv, pow2_at_least(std::max<long long>(2LL * c->max_zone, zmin)));
+  const long long smin = es ? std::max(1LL, std::atoll(es)) : 65536, zmin = ez ? std::max(1LL, std::atoll(ez)) : 16384;
+  const long long smul = es ? 2 : 4, zmul = ez ? 2 : 4;
+  c->g_scand = std::min(c->C.cand_cap, pow2_at_least(std::max<long long>(smul * c->max_ncand, smin)));
+  c->g_szone = std::min(A.nv, pow2_at_least(std::max<long long>(zmul * c->max_zone, zmin)));
   {
     int dev = 0, sms = 0;
     CK(cudaGetDevice(&dev));
@@ -451,6 +455,8 @@ bool graph_frame(cs_ctx* c, const std::vector<int>& act) {
     CK(cudaStreamSynchronize(c->stream));
     graph_release(c);
     c->g_overflows++;
+    for (int k = 0; k < 4; k++)
+      if (ctl.overflow & (1 << k)) c->g_over_reason[k]++;
     return false;
   }
   note_divergence(c);

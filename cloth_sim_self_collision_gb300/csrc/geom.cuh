@@ -405,7 +405,7 @@ __device__ __forceinline__ bool fv_sign_reject32(V3<double> e1, V3<double> e2, V
 
 // Closest points of segments a0 a1 and b0 b1 (FP32, clamped): the vector from
 // the point on a to the point on b.  Only a direction for the certificate below.
-__device__ __forceinline__ void seg_seg_dir32(const float a0[3], const float a1[3], const float b0[3],
+CS_HD void seg_seg_dir32(const float a0[3], const float a1[3], const float b0[3],
                                               const float b1[3], float d[3]) {
   float u[3], v[3], w[3];
 #pragma unroll

@@ -22,6 +22,7 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include "cert.cuh"
 #include "kernels.h"
 
 namespace cs {
@@ -459,8 +460,8 @@ __global__ void __launch_bounds__(kT) k_narrow_filter_dev(Arena A, ContactBufs C
 }
 
 // pass 2, face-vertex tests (grid-stride over their queue)
-__global__ void k_narrow_fv(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs,
-                            double delta_override) {
+__device__ __forceinline__ void narrow_fv_body(const Arena& A, const ContactBufs& C, int ccd, const double* xs,
+                                               const double* vs, double delta_override) {
   const int n = min(__ldcg(&C.counters[6]), C.q_cap[0]);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int2 it = C.queue[0][i];
@@ -483,27 +484,60 @@ __global__ void k_narrow_fv(Arena A, ContactBufs C, int ccd, const double* xs, c
     } else {
       const V3<double> q0 = end_pos(xs, vs, f0, P.dt), q1 = end_pos(xs, vs, f1, P.dt);
       const V3<double> q2 = end_pos(xs, vs, f2, P.dt), q3 = end_pos(xs, vs, q, P.dt);
-      {
-        // FP32 certificates that the FP64 test rejects: the vertex stays on one
-        // side of the start face plane (the test's sign block), or the four
-        // points are never coplanar in [0, 1] (FindCoplanerInterp returns -1);
-        // both from the FP64 differences the FP64 test itself forms
-        const V3<double> x1 = p1 - p0, x2 = p2 - p0;
-        if (fv_sign_reject32(x1, x2, p0 - p3, q0 - q3, q1 - q3, q2 - q3)) continue;
-        const V3<double> x3 = p3 - p0;
-        const V3<double> v1 = (q1 - q0) - x1, v2 = (q2 - q0) - x2, v3 = (q3 - q0) - x3;
-        if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
-      }
-      count_fp64_test(A, 4);
-      const Box bb = A.box[fa ? na : nb];
-      if (fv_ccd(f0, f1, f2, q, p0, p1, p2, p3, q0, q1, q2, q3, bb)) emit(C, 1, f0, f1, f2, q, na, nb, test);
+      // FP32 certificates that the FP64 test rejects: the vertex stays on one
+      // side of the start face plane (the test's sign block), the four points
+      // are never coplanar in [0, 1] (FindCoplanerInterp returns -1), or at any
+      // coplanarity time the vertex projects outside the face (cert.cuh); all
+      // from the FP64 differences the FP64 test itself forms
+      const V3<double> x1 = p1 - p0, x2 = p2 - p0;
+      if (fv_sign_reject32(x1, x2, p0 - p3, q0 - q3, q1 - q3, q2 - q3)) continue;
+      const V3<double> x3 = p3 - p0;
+      const V3<double> v1 = (q1 - q0) - x1, v2 = (q2 - q0) - x2, v3 = (q3 - q0) - x3;
+      if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
+      if (fv_ccd_pieces32(x1, x2, x3, v1, v2, v3)) continue;
+      // left to the FP64 test (k_narrow_fv64), in a packed queue
+      C.queue64[0][warp_append(&C.counters[10])] = it;
     }
   }
 }
 
-// pass 2, edge-edge tests (grid-stride over their queue)
-__global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs,
+// the face-vertex continuous-collision tests the certificates left (FP64)
+__device__ __forceinline__ void narrow_fv64_body(const Arena& A, const ContactBufs& C, const double* xs,
+                                                 const double* vs) {
+  const int n = __ldcg(&C.counters[10]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 it = C.queue64[0][i];
+    const int2 pr = C.pairs[it.x];
+    const int na = pr.x, nb = pr.y, test = it.y;
+    const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
+    const DevParams& P = A.prm[A.tinst[ta]];
+    const bool fa = test < 3;
+    const int tf = fa ? ta : tb, tv = fa ? tb : ta, k = fa ? test : test - 3;
+    const int f0 = A.tri[3 * tf], f1 = A.tri[3 * tf + 1], f2 = A.tri[3 * tf + 2], q = A.tri[3 * tv + k];
+    const V3<double> p0 = ld3(xs, f0), p1 = ld3(xs, f1), p2 = ld3(xs, f2), p3 = ld3(xs, q);
+    const V3<double> q0 = end_pos(xs, vs, f0, P.dt), q1 = end_pos(xs, vs, f1, P.dt);
+    const V3<double> q2 = end_pos(xs, vs, f2, P.dt), q3 = end_pos(xs, vs, q, P.dt);
+    count_fp64_test(A, 4);
+    const Box bb = A.box[fa ? na : nb];
+    if (fv_ccd(f0, f1, f2, q, p0, p1, p2, p3, q0, q1, q2, q3, bb)) emit(C, 1, f0, f1, f2, q, na, nb, test);
+  }
+}
+
+// the face-vertex pass as compiled freely (about 164 registers) and capped at
+// 128 registers for 4 blocks per SM (more warps in flight, a few spills):
+// the autotuner picks one per arena (Arena::narrow_regs)
+__global__ void k_narrow_fv(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs,
                             double delta_override) {
+  narrow_fv_body(A, C, ccd, xs, vs, delta_override);
+}
+__global__ void __launch_bounds__(kT, 4) k_narrow_fv_b4(Arena A, ContactBufs C, int ccd, const double* xs,
+                                                        const double* vs, double delta_override) {
+  narrow_fv_body(A, C, ccd, xs, vs, delta_override);
+}
+
+// pass 2, edge-edge tests (grid-stride over their queue)
+__device__ __forceinline__ void narrow_ee_body(const Arena& A, const ContactBufs& C, int ccd, const double* xs,
+                                               const double* vs, double delta_override) {
   const int n = min(__ldcg(&C.counters[7]), C.q_cap[1]);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int2 it = C.queue[1][i];
@@ -525,18 +559,92 @@ __global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, c
     } else {
       const V3<double> p0e = end_pos(xs, vs, i0, P.dt), p1e = end_pos(xs, vs, i1, P.dt);
       const V3<double> q0e = end_pos(xs, vs, j0, P.dt), q1e = end_pos(xs, vs, j1, P.dt);
-      {
-        // no coplanarity in [0, 1]: the vectors coplanar_time forms, in FP64 as it does
-        const V3<double> x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0;
-        const V3<double> v1 = (p1e - p0e) - x1, v2 = (q0e - p0e) - x2, v3 = (q1e - p0e) - x3;
-        if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
-      }
+      // no coplanarity in [0, 1]: the vectors coplanar_time forms, in FP64 as it does
+      const V3<double> x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0;
+      const V3<double> v1 = (p1e - p0e) - x1, v2 = (q0e - p0e) - x2, v3 = (q1e - p0e) - x3;
+      if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
       // the edges stay more than the test's 1e-2 apart over the whole motion
       if (ee_ccd_far32(p0, p1, q0, q1, p0e, p1e, q0e, q1e, 1.0e-2)) continue;
-      count_fp64_test(A, 5);
-      if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, p0e, p1e, q0e, q1e)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
+      // at any coplanarity time a ratio is out of range or the edges are apart
+      if (ee_ccd_pieces32(x1, x2, x3, v1, v2, v3)) continue;
+      C.queue64[1][warp_append(&C.counters[11])] = it;
     }
   }
+}
+
+// the edge-edge continuous-collision tests the certificates left (FP64)
+__device__ __forceinline__ void narrow_ee64_body(const Arena& A, const ContactBufs& C, const double* xs,
+                                                 const double* vs) {
+  const int n = __ldcg(&C.counters[11]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 it = C.queue64[1][i];
+    const int2 pr = C.pairs[it.x];
+    const int na = pr.x, nb = pr.y, test = it.y;
+    const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
+    const DevParams& P = A.prm[A.tinst[ta]];
+    const int k = test - 6;
+    const int i0 = A.tri[3 * ta + kEE[k][0]], i1 = A.tri[3 * ta + kEE[k][1]];
+    const int j0 = A.tri[3 * tb + kEE[k][2]], j1 = A.tri[3 * tb + kEE[k][3]];
+    const V3<double> p0 = ld3(xs, i0), p1 = ld3(xs, i1), q0 = ld3(xs, j0), q1 = ld3(xs, j1);
+    const V3<double> p0e = end_pos(xs, vs, i0, P.dt), p1e = end_pos(xs, vs, i1, P.dt);
+    const V3<double> q0e = end_pos(xs, vs, j0, P.dt), q1e = end_pos(xs, vs, j1, P.dt);
+    count_fp64_test(A, 5);
+    if (ee_ccd(i0, i1, j0, j1, p0, p1, q0, q1, p0e, p1e, q0e, q1e)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
+  }
+}
+
+__global__ void k_narrow_ee(Arena A, ContactBufs C, int ccd, const double* xs, const double* vs,
+                            double delta_override) {
+  narrow_ee_body(A, C, ccd, xs, vs, delta_override);
+}
+__global__ void __launch_bounds__(kT, 4) k_narrow_ee_b4(Arena A, ContactBufs C, int ccd, const double* xs,
+                                                        const double* vs, double delta_override) {
+  narrow_ee_body(A, C, ccd, xs, vs, delta_override);
+}
+__global__ void k_narrow_fv64(Arena A, ContactBufs C, const double* xs, const double* vs) {
+  narrow_fv64_body(A, C, xs, vs);
+}
+__global__ void __launch_bounds__(kT, 4) k_narrow_fv64_b4(Arena A, ContactBufs C, const double* xs,
+                                                          const double* vs) {
+  narrow_fv64_body(A, C, xs, vs);
+}
+__global__ void k_narrow_ee64(Arena A, ContactBufs C, const double* xs, const double* vs) {
+  narrow_ee64_body(A, C, xs, vs);
+}
+__global__ void __launch_bounds__(kT, 4) k_narrow_ee64_b4(Arena A, ContactBufs C, const double* xs,
+                                                          const double* vs) {
+  narrow_ee64_body(A, C, xs, vs);
+}
+
+// The passes after the FP32 prefilter, in the arena's register variant:
+// face-vertex and edge-edge tests (proximity: the FP64 tests; continuous
+// collision: the FP32 certificates, then the FP64 tests they leave, packed)
+void narrow_fp64_passes(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
+                        double delta_override, int grid, cudaStream_t s) {
+  const bool b4 = A.narrow_regs == 128;
+  prof_begin(PK_NARROW_FV, s);
+  if (b4)
+    k_narrow_fv_b4<<<grid, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
+  else
+    k_narrow_fv<<<grid, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
+  prof_end(PK_NARROW_FV, s);
+  prof_begin(PK_NARROW_EE, s);
+  if (b4)
+    k_narrow_ee_b4<<<grid, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
+  else
+    k_narrow_ee<<<grid, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
+  prof_end(PK_NARROW_EE, s);
+  if (!ccd) return;
+  prof_begin(PK_NARROW_CCD64, s);
+  if (b4) {
+    k_narrow_fv64_b4<<<grid, kT, 0, s>>>(A, C, xs, vs);
+    k_narrow_ee64_b4<<<grid, kT, 0, s>>>(A, C, xs, vs);
+  } else {
+    k_narrow_fv64<<<grid, kT, 0, s>>>(A, C, xs, vs);
+    k_narrow_ee64<<<grid, kT, 0, s>>>(A, C, xs, vs);
+  }
+  prof_end(PK_NARROW_CCD64, s);
+  g_launches += 2;
 }
 
 __device__ __forceinline__ unsigned long long key_hi(const Cand& c) {
@@ -1042,16 +1150,11 @@ void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* 
     grid2 = 8 * (sms > 0 ? sms : 1);
   }
   prof_begin(PK_NARROW, s);
-  cudaMemsetAsync(C.counters + 6, 0, 2 * sizeof(int), s);
+  cudaMemsetAsync(C.counters + 6, 0, 6 * sizeof(int), s);  // queue counts [6, 7], [10, 11]
   prof_begin(PK_NARROW_FILTER, s);
   k_narrow_filter<<<nblk(npairs), kT, 0, s>>>(A, C, ccd, delta_override, npairs);
   prof_end(PK_NARROW_FILTER, s);
-  prof_begin(PK_NARROW_FV, s);
-  k_narrow_fv<<<grid2, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
-  prof_end(PK_NARROW_FV, s);
-  prof_begin(PK_NARROW_EE, s);
-  k_narrow_ee<<<grid2, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
-  prof_end(PK_NARROW_EE, s);
+  narrow_fp64_passes(A, C, ccd, xs, vs, delta_override, grid2, s);
   prof_end(PK_NARROW, s);
   g_launches += 3;
 }
@@ -1286,7 +1389,7 @@ __global__ void k_sort_prep(Arena A, ContactBufs C, int S) {
   const bool over = n > S || n > C.cand_cap;
   C.counters[8] = over ? 0 : n;
   C.counters[2] = 0;
-  if (over) A.ctl->overflow = 1;
+  if (over) A.ctl->overflow |= kOverflowSort;
 }
 
 __global__ void k_keys_lo_pad(ContactBufs C, int S) {
@@ -1351,7 +1454,7 @@ __global__ void k_compact_dev(ContactBufs C, int S) {
 // overflow flag of the broad and narrow phases
 __global__ void k_detect_done(Arena A, ContactBufs C) {
   FrameCtl* c = A.ctl;
-  if (C.counters[3]) c->overflow = 1;
+  if (C.counters[3]) c->overflow |= kOverflowBuffers;
   c->last_ncand = C.counters[8];
   c->last_nce = C.counters[2];
 }
@@ -1373,7 +1476,7 @@ __global__ void k_riz_contacts_dev(Arena A, ContactBufs C) {
 __global__ void k_zone_prep(Arena A, ContactBufs C, int S) {
   const int n = C.counters[4];
   const bool over = n > S;
-  if (over) A.ctl->overflow = 1;
+  if (over) A.ctl->overflow |= kOverflowZone;
   C.counters[9] = over ? 0 : n;
 }
 
@@ -1396,10 +1499,9 @@ __global__ void k_riz_velocity_dev(ContactBufs C, int S, const double* xs, doubl
 
 void launch_narrow_dev(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
                        cudaStream_t s) {
-  launch_check(cudaMemsetAsync(C.counters + 6, 0, 2 * sizeof(int), s), "cudaMemsetAsync");
+  launch_check(cudaMemsetAsync(C.counters + 6, 0, 6 * sizeof(int), s), "cudaMemsetAsync");
   k_narrow_filter_dev<<<dev_grid(A), kT, 0, s>>>(A, C, ccd, -1.0);
-  k_narrow_fv<<<dev_grid(A), kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
-  k_narrow_ee<<<dev_grid(A), kT, 0, s>>>(A, C, ccd, xs, vs, -1.0);
+  narrow_fp64_passes(A, C, ccd, xs, vs, -1.0, dev_grid(A), s);
   g_launches += 3;
 }
 

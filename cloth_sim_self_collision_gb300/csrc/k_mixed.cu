@@ -721,19 +721,33 @@ __global__ void k_mx_correct(Arena A) {
   }
 }
 
-// r = b - A dx with the FP64 matrix (the product by 16-lane groups into r, then
-// one thread per row); chunk partials of r.r
+// r = b - A dx with the FP64 matrix, one thread per row; chunk partials of r.r.
+// GB300 issues FP64 at 2 lanes per clock per SM, so this product is bound by
+// the FP64 pipe, not by HBM: the row's in-order sum must stay on one lane (a
+// row split over lanes pays the sequential adds on every lane of the group).
 __global__ void __launch_bounds__(kChunk) k_mx_residual(Arena A) {
   __shared__ double sh[33];
   const int c = blockIdx.x;
   const int inst = A.chunk_inst[c];
   if (!A.active[inst] || A.st[inst].done) return;
   const int i = chunk_row(A, c, inst);
-  const int r0c = i - (int)threadIdx.x;
-  spmv_rows_coop(A, r0c, min(r0c + kChunk, A.voff[inst + 1]), A.dx, A.r, true);
   double s = 0.0;
   if (i < A.voff[inst + 1]) {
-    const double y0 = A.r[3 * i + 0], y1 = A.r[3 * i + 1], y2 = A.r[3 * i + 2];
+    double y0 = 0.0, y1 = 0.0, y2 = 0.0;
+    const double* x = A.dx;
+    for (int k = A.row_ptr[i]; k < A.row_ptr[i + 1]; k++) {
+      const int j = A.col_idx[k];
+      const double* a = A.vcrs + 9 * (size_t)k;
+      const double x0 = x[3 * j + 0], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+      y0 += a[0] * x0 + a[1] * x1 + a[2] * x2;
+      y1 += a[3] * x0 + a[4] * x1 + a[5] * x2;
+      y2 += a[6] * x0 + a[7] * x1 + a[8] * x2;
+    }
+    const double* a = A.vdia + 9 * (size_t)i;
+    const double x0 = x[3 * i + 0], x1 = x[3 * i + 1], x2 = x[3 * i + 2];
+    y0 += a[0] * x0 + a[1] * x1 + a[2] * x2;
+    y1 += a[3] * x0 + a[4] * x1 + a[5] * x2;
+    y2 += a[6] * x0 + a[7] * x1 + a[8] * x2;
     const double r0 = A.b[3 * i + 0] - y0, r1 = A.b[3 * i + 1] - y1, r2 = A.b[3 * i + 2] - y2;
     A.r[3 * i + 0] = r0;
     A.r[3 * i + 1] = r1;

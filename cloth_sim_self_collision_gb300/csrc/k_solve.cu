@@ -451,18 +451,17 @@ __global__ void k_cg_start(Arena A, double tol_in, int maxit_in) {
   }
 }
 
-// Ap = A p and the chunk partials of p.Ap (the product by 16-lane groups, the
-// partials one thread per row as before)
+// Ap = A p and the chunk partials of p.Ap, one thread per row (FP64-pipe bound
+// on GB300; the row's in-order sum stays on one lane)
 __global__ void __launch_bounds__(kChunk) k_cg_spmv(Arena A) {
   __shared__ double sh[40];
   const int c = blockIdx.x;
   const int inst = A.chunk_inst[c];
   if (!A.active[inst] || A.st[inst].done) return;
-  const int r0 = A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk;
-  const int row = r0 + threadIdx.x;
-  spmv_rows_coop(A, r0, min(r0 + kChunk, A.voff[inst + 1]), A.p, A.z);
+  const int row = A.voff[inst] + (c - A.chunk_lo[inst]) * kChunk + threadIdx.x;
   double s = 0.0;
   if (row < A.voff[inst + 1]) {
+    spmv_row(A, row, A.p, A.z);
     s = A.p[3 * row + 0] * A.z[3 * row + 0] + A.p[3 * row + 1] * A.z[3 * row + 1] +
         A.p[3 * row + 2] * A.z[3 * row + 2];
   }

@@ -31,58 +31,6 @@ inline void launch_check(cudaError_t e, const char* what) {
 // launches issued by this process (all contexts), for launch accounting
 extern std::atomic<long long> g_launches;
 
-// y_i = 0 * y_i + sum_j A_ij x_j (MatVec(1, x, 0, y), matrix_square_sparse.cpp:218-242)
-// for the rows [r0, r1) by a block of 256 threads, 16 lanes per row: lane j
-// forms slot j's three row products with the reference's grouping, and the
-// row's first lane adds them in slot order, then the diagonal block, so every
-// result equals the one-thread-per-row loop bit for bit.  zero_start: each row
-// starts from 0.0 instead of 0 * y_i.  Ends with __syncthreads.
-__device__ __forceinline__ void spmv_rows_coop(const Arena& A, int r0, int r1, const double* x, double* y,
-                                               bool zero_start = false) {
-  const int g = threadIdx.x >> 4, l = threadIdx.x & 15;
-  const unsigned mask = 0xffffu << (threadIdx.x & 16);
-  for (int i = r0 + g; i < r1; i += (int)(blockDim.x >> 4)) {
-    const int s0 = A.row_ptr[i], s1 = A.row_ptr[i + 1];
-    double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-    if (l == 0 && !zero_start) {
-      y0 = y[3 * i + 0] * 0.0;
-      y1 = y[3 * i + 1] * 0.0;
-      y2 = y[3 * i + 2] * 0.0;
-    }
-    for (int base = s0; base < s1; base += 16) {
-      const int s = base + l;
-      double d0 = 0.0, d1 = 0.0, d2 = 0.0;
-      if (s < s1) {
-        const int j = A.col_idx[s];
-        const double* a = A.vcrs + 9 * (size_t)s;
-        const double x0 = x[3 * j + 0], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
-        d0 = a[0] * x0 + a[1] * x1 + a[2] * x2;
-        d1 = a[3] * x0 + a[4] * x1 + a[5] * x2;
-        d2 = a[6] * x0 + a[7] * x1 + a[8] * x2;
-      }
-      const int m = min(16, s1 - base);
-      for (int q = 0; q < m; q++) {
-        const double e0 = __shfl_sync(mask, d0, q, 16), e1 = __shfl_sync(mask, d1, q, 16),
-                     e2 = __shfl_sync(mask, d2, q, 16);
-        y0 += 1.0 * e0;
-        y1 += 1.0 * e1;
-        y2 += 1.0 * e2;
-      }
-    }
-    if (l == 0) {
-      const double* a = A.vdia + 9 * (size_t)i;
-      const double x0 = x[3 * i + 0], x1 = x[3 * i + 1], x2 = x[3 * i + 2];
-      y0 += 1.0 * (a[0] * x0 + a[1] * x1 + a[2] * x2);
-      y1 += 1.0 * (a[3] * x0 + a[4] * x1 + a[5] * x2);
-      y2 += 1.0 * (a[6] * x0 + a[7] * x1 + a[8] * x2);
-      y[3 * i + 0] = y0;
-      y[3 * i + 1] = y1;
-      y[3 * i + 2] = y2;
-    }
-  }
-  __syncthreads();
-}
-
 // --- assembly (k_assemble.cu) ---------------------------------------------
 void launch_quad_factors(const Arena& A, cudaStream_t s);
 // element gradients (and Hessian blocks when hess) at positions A.x; masked:

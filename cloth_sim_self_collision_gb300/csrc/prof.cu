@@ -11,7 +11,7 @@ const char* const kProfNames[PK_COUNT] = {"tri_elements", "slot_reduce", "rhs", 
                                           "refit",        "traverse",    "narrow",    "impulse",
                                           "mx_spmv",      "mx_update",   "mx_direction", "mx_residual",
                                           "mx_persist",   "narrow_filter", "narrow_fv", "narrow_ee",
-                                          "sort"};
+                                          "sort",         "narrow_ccd64"};
 
 namespace {
 struct Pending {

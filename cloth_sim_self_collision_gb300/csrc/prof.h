@@ -27,6 +27,7 @@ enum ProfKernel {
   PK_NARROW_FV,
   PK_NARROW_EE,
   PK_SORT,
+  PK_NARROW_CCD64,
   PK_COUNT
 };
 

@@ -351,12 +351,19 @@ int cs_set_frame_mode(cs_ctx *ctx, int mode);
  * outgrew a fixed size (each then re-run host-driven); any pointer may be null. */
 int cs_frame_counts(cs_ctx *ctx, long long *graph_frames, long long *host_frames, long long *captures,
                     long long *overflows);
+/* The graph frames re-run host-driven, by reason (a frame may count under
+ * several): reasons[0] candidates beyond the graph's padded sort size,
+ * [1] impact-zone members beyond its padded sort size, [2] leaf pairs, test
+ * queues or candidates beyond the contact buffers (which the host-driven frame
+ * then grows), [3] refinement cycles beyond the graph's cap. */
+int cs_frame_overflows(cs_ctx *ctx, long long reasons[4]);
 
 /* ---- autotuning of launch shapes ----------------------------------------------------- */
 /* No counterpart in the reference.  Times `frames` frames from the current state
  * for candidate launch shapes (coordinate descent over the persistent solver's
  * blocks per SM, the slice count below which it continues in a smaller tail
- * launch, and the blocks per SM of the narrow-phase kernels of graph frames),
+ * launch, the blocks per SM of the narrow-phase kernels of graph frames, and
+ * whether the FP64 narrow-phase kernels are capped at 128 registers),
  * restoring the state after each, and keeps the fastest.  The frames do not
  * depend on these shapes, so the simulation continues exactly where it was.
  * Results are cached per arena shape (cloths, vertices, slices, precision) for
@@ -365,6 +372,7 @@ typedef struct cs_tune_result {
   int mx_blocks_per_sm;   /* persistent solver: blocks of 256 threads per SM    */
   int mx_tail_slices;     /* persistent solver: tail launch threshold (0: none)  */
   int graph_grid_per_sm;  /* graph frames: narrow-phase blocks per SM           */
+  int narrow_regs;        /* FP64 narrow-phase kernels: 0 free, 128 capped       */
   double frame_ms;        /* measured time of a frame with these shapes         */
   int candidates;         /* configurations timed                               */
   int cached;             /* 1: taken from an earlier call on the same shape    */

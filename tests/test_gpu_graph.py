@@ -84,6 +84,17 @@ def test_graph_overflow_rerun_and_recapture(monkeypatch):
     assert g[2]["overflows"] > 0 and g[2]["captures"] > 1 and g[2]["graph_frames"] > 0, g[2]
 
 
+def test_narrow_register_variants_equal(monkeypatch):
+    """The FP64 narrow-phase kernels capped at 128 registers (a variant the
+    autotuner may pick) find the same contacts: frames equal bit for bit."""
+    cl = scene.config_batch(count=16)
+    a = run(cl, "mixed", True, 40)
+    monkeypatch.setenv("CLOTHGPU_NARROW_REGS", "128")
+    b = run(cl, "mixed", True, 40)
+    assert same(a, b)
+    assert sum(s["n_ccd"] > 0 for fr in b[1] for s in fr) > 0
+
+
 def test_autotune_leaves_frames_unchanged():
     """cs_autotune times candidate launch shapes on frames from the current state
     and restores it: the frames that follow equal those of an untuned context
@@ -113,3 +124,4 @@ def test_autotune_leaves_frames_unchanged():
     assert t0["cached"] == 0 and t0["candidates"] >= 3 and t0["frame_ms"] > 0
     assert t1["cached"] == 1 and t1["mx_blocks_per_sm"] == t0["mx_blocks_per_sm"]
     assert t0["mx_blocks_per_sm"] in (4, 5, 6) and t0["graph_grid_per_sm"] in (4, 8, 16)
+    assert t0["narrow_regs"] in (0, 128)
