@@ -1697,6 +1697,27 @@ double co_coplanar_time(const double *s, const double *e) {
   return coplanar_time(at(s, 0), at(s, 1), at(s, 2), at(s, 3), at(e, 0), at(e, 1), at(e, 2), at(e, 3));
 }
 
+void co_fv_ccd_batch(int n, const double *p, const double *box, int *out) {
+  box3 bb;
+  int i, k;
+  for (k = 0; k < 3; k++) {
+    bb.lo[k] = box[k];
+    bb.hi[k] = box[3 + k];
+  }
+  bb.full = 1;
+  for (i = 0; i < n; i++) {
+    const double *a = p + 24 * (size_t)i;
+    out[i] = fv_ccd(0, 1, 2, 3, at(a, 0), at(a, 1), at(a, 2), at(a, 3), at(a, 4), at(a, 5), at(a, 6), at(a, 7), &bb);
+  }
+}
+void co_ee_ccd_batch(int n, const double *p, int *out) {
+  int i;
+  for (i = 0; i < n; i++) {
+    const double *a = p + 24 * (size_t)i;
+    out[i] = ee_ccd(0, 1, 2, 3, at(a, 0), at(a, 1), at(a, 2), at(a, 3), at(a, 4), at(a, 5), at(a, 6), at(a, 7));
+  }
+}
+
 int co_contacts_prx(co_cloth *h, const double *x, double delta, int *out, int cap) {
   co_refit_prx(h, x, delta, NULL);
   return collect(h, x, NULL, 0, delta, 0, out, cap);

@@ -110,6 +110,12 @@ void co_matvec(const co_cloth *h, double alpha, const double *x, double beta, do
 double co_distance_fv(const double *p, double *w);
 double co_distance_ee(const double *p, double *r);
 double co_coplanar_time(const double *s, const double *e);
+/* IsContact_FV_CCD / IsContact_EE_CCD on n configurations of 24 doubles each
+ * (start points, then end points: face p0 p1 p2 and vertex p3, or edges p0 p1
+ * and q0 q1), with the distinct indices 0..3; the face-vertex test takes the box
+ * (lo[3], hi[3]) for its node; results (0 or 1) into out */
+void co_fv_ccd_batch(int n, const double *p, const double *box, int *out);
+void co_ee_ccd_batch(int n, const double *p, int *out);
 
 /* collision pieces */
 void co_refit_prx(co_cloth *h, const double *x, double delta, double *boxes);

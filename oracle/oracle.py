@@ -148,6 +148,8 @@ class OracleLib:
         self.distance_fv = f("distance_fv", ctypes.c_double, _D, _D)
         self.distance_ee = f("distance_ee", ctypes.c_double, _D, _D)
         self.coplanar_time = f("coplanar_time", ctypes.c_double, _D, _D)
+        self.fv_ccd_batch = f("fv_ccd_batch", None, ctypes.c_int, _D, _D, _I)
+        self.ee_ccd_batch = f("ee_ccd_batch", None, ctypes.c_int, _D, _I)
         # contact log (restatement only: the reference keeps no per-pass record)
         self.has_log = hasattr(L, pre + "contact_log")
         if self.has_log:
@@ -411,3 +413,23 @@ def coplanar_time(lib: OracleLib, s, e):
     """FindCoplanerInterp on start / end points (12 doubles each)."""
     return lib.coplanar_time(_dp(np.ascontiguousarray(s, dtype=np.float64)),
                              _dp(np.ascontiguousarray(e, dtype=np.float64)))
+
+
+def fv_ccd(lib: OracleLib, pts, box=None) -> np.ndarray:
+    """IsContact_FV_CCD on configurations (n, 24): start face p0 p1 p2, vertex
+    p3, then their end points; box (6: lo, hi) for the face's node, by default
+    one that holds everything.  0 / 1 per configuration."""
+    p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 24)
+    b = np.ascontiguousarray(box if box is not None else [-1e30] * 3 + [1e30] * 3, dtype=np.float64)
+    out = np.zeros(len(p), dtype=np.int32)
+    lib.fv_ccd_batch(len(p), _dp(p), _dp(b), out.ctypes.data_as(_I))
+    return out
+
+
+def ee_ccd(lib: OracleLib, pts) -> np.ndarray:
+    """IsContact_EE_CCD on configurations (n, 24): start edges p0 p1, q0 q1,
+    then their end points.  0 / 1 per configuration."""
+    p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 24)
+    out = np.zeros(len(p), dtype=np.int32)
+    lib.ee_ccd_batch(len(p), _dp(p), out.ctypes.data_as(_I))
+    return out

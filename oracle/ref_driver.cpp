@@ -35,6 +35,12 @@ void SelfCollisionImpulse_CCD(std::vector<double>& aUVWm, double delta, double s
                               double dt, double mass, const std::vector<double>& aXYZ,
                               const std::vector<int>& aTri,
                               const std::vector<CContactElement>& aContactElem);
+bool IsContact_FV_CCD(int ino0, int ino1, int ino2, int ino3, const CVector3D& p0, const CVector3D& p1,
+                      const CVector3D& p2, const CVector3D& p3, const CVector3D& q0, const CVector3D& q1,
+                      const CVector3D& q2, const CVector3D& q3, const CAABB3D& bb);
+bool IsContact_EE_CCD(int ino0, int ino1, int jno0, int jno1, const CVector3D& p0s, const CVector3D& p1s,
+                      const CVector3D& q0s, const CVector3D& q1s, const CVector3D& p0e, const CVector3D& p1e,
+                      const CVector3D& q0e, const CVector3D& q1e);
 void MakeRigidImpactZone(std::vector<std::set<int> >& aRIZ,
                          const std::vector<CContactElement>& aContactElem,
                          const CJaggedArray& aEdge);
@@ -369,6 +375,23 @@ double ref_distance_ee(const double* pt, double* r) {
 
 double ref_coplanar_time(const double* s, const double* e) {
   return FindCoplanerInterp(v3(s, 0), v3(s, 1), v3(s, 2), v3(s, 3), v3(e, 0), v3(e, 1), v3(e, 2), v3(e, 3));
+}
+
+void ref_fv_ccd_batch(int n, const double* p, const double* box, int* out) {
+  const CAABB3D bb(box[0], box[3], box[1], box[4], box[2], box[5]);
+  for (int i = 0; i < n; i++) {
+    const double* a = p + 24 * (size_t)i;
+    out[i] = IsContact_FV_CCD(0, 1, 2, 3, v3(a, 0), v3(a, 1), v3(a, 2), v3(a, 3), v3(a, 4), v3(a, 5), v3(a, 6),
+                              v3(a, 7), bb);
+  }
+}
+
+void ref_ee_ccd_batch(int n, const double* p, int* out) {
+  for (int i = 0; i < n; i++) {
+    const double* a = p + 24 * (size_t)i;
+    out[i] = IsContact_EE_CCD(0, 1, 2, 3, v3(a, 0), v3(a, 1), v3(a, 2), v3(a, 3), v3(a, 4), v3(a, 5), v3(a, 6),
+                              v3(a, 7));
+  }
 }
 
 // StepTime_InternalDynamicsILU / StepTime_InternalDynamics with the solver tolerance

@@ -143,3 +143,20 @@ def test_geometry_functions_match_reference(oracle_port, oracle_ref):
         if k % 7 == 0:  # equal displacement of all points: the cubic degenerates
             e = p + np.tile(rng.normal(0, 0.2, 3), 4)
         assert O.coplanar_time(oracle_port, p, e) == O.coplanar_time(oracle_ref, p, e)
+
+
+def test_ccd_tests_match_reference(oracle_port, oracle_ref):
+    """IsContact_FV_CCD and IsContact_EE_CCD on the configurations the
+    certificate tests use (sheet patches, crossing sheets, exactly flat
+    sheets, random): the restatement's decisions equal the reference's."""
+    import test_ccd_certificates as T
+    for kind in ("fv", "ee"):
+        for i, (name, make) in enumerate(T.SCENARIOS.items()):
+            cfg = make(np.random.default_rng(500 + 10 * i + (kind == "ee")), kind)
+            if kind == "fv":
+                box = np.array([-0.3, -0.3, -0.3, 0.3, 0.3, 0.3])
+                a, b = O.fv_ccd(oracle_port, cfg, box), O.fv_ccd(oracle_ref, cfg, box)
+            else:
+                a, b = O.ee_ccd(oracle_port, cfg), O.ee_ccd(oracle_ref, cfg)
+            assert np.array_equal(a, b), (kind, name, np.nonzero(a != b)[0][:5])
+            assert 0 < b.sum() or name in ("sheet", "flat")
