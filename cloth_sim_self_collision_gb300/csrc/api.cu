@@ -946,7 +946,9 @@ size_t cloth_device_bytes(const ClothTopo& t) {
   const size_t sell = ((np + 31) / 32) * 32 * 16;  // SELL entries, padded to the slice width
   b += sell * (36 + 4) + (nb + np) * 8;        // FP32 values, columns, SELL positions
   b += np * (36 + 5 * 12);                     // FP32 diagonal inverse and vectors
-  b += (16 * nt + 4096) * 8 * 7 / 2 + (4 * nt + 4096) * 120;  // pair, test-queue and candidate buffers
+  // pairs, the test queues and their FP64 queues (2.5 pair capacities each),
+  // and the candidate buffers
+  b += (16 * nt + 4096) * 8 * 6 + (4 * nt + 4096) * 120;
   b += np * (2 * 4 + 2 * 8 + 72);              // vertex marks, zone keys and sums
   return b + (1 << 16);
 }

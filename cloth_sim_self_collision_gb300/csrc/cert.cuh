@@ -7,10 +7,11 @@
 // certificates below bound those ratios and that distance over whole
 // sub-intervals of [0, 1], so they reject a test without knowing t:
 //
-// the coplanarity cubic's roots are localised to the pieces (of eight) on which
-// its Bernstein coefficients do not keep one sign; the reference's bisection
-// returns a t within 2^-15 of a sign change of its FP64 cubic, so only those
-// pieces, widened by 2^-14, can hold t; on each:
+// the coplanarity cubic's roots are localised to the pieces (eighths, halved
+// down to 1/32 where needed) on which its Bernstein coefficients do not keep
+// one sign; the reference's bisection returns a t within 2^-15 of a sign change
+// of its FP64 cubic, so only those pieces, widened by 2^-14, can hold t; on
+// each:
 // * face-vertex: one barycentric ratio of the vertex's projection stays
 //   outside [0, 1];
 // * edge-edge: one ratio stays outside [0, 1], or the lines stay more than
@@ -244,6 +245,30 @@ CS_HD bool ee_piece_reject32(const RV& x1, const RV& x2, const RV& x3, const RV&
   return gap > need;
 }
 
+// True when t cannot lie in [a, a + h] (a, h exact), or the test rejects at
+// every t there: the cubic k keeps one sign on the piece beyond the reference's
+// FP64 evaluation error F (its Bernstein coefficients), so its bisection ends
+// elsewhere, unless the piece ends at 1 and k0 may vanish; otherwise the
+// piece, widened by 2^-14 on each side, passes the face-vertex or edge-edge
+// certificate.
+template <bool kFV>
+CS_HD bool piece_clear(const R32 k[4], float F, bool k0_zero, float a, float h, const RV& x1, const RV& x2,
+                       const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
+  const R32 third = rc(0.33333334f, 1.0e-8f), two_thirds = rc(0.6666667f, 3.0e-8f);
+  const R32 K0 = k[0] + a * (k[1] + a * (k[2] + a * k[3]));
+  const R32 K1 = h * (k[1] + a * (2.f * k[2] + (3.f * a) * k[3]));
+  const R32 K2 = (h * h) * (k[2] + (3.f * a) * k[3]);
+  const R32 K3 = (h * h * h) * k[3];
+  const R32 B1 = K0 + third * K1, B2 = (K0 + two_thirds * K1) + third * K2, B3 = ((K0 + K1) + K2) + K3;
+  const bool pos = lo32(K0) > F && lo32(B1) > F && lo32(B2) > F && lo32(B3) > F;
+  const bool neg = hi32(K0) < -F && hi32(B1) < -F && hi32(B2) < -F && hi32(B3) < -F;
+  if ((pos || neg) && !(k0_zero && a + h == 1.f)) return true;
+  const float eps = 6.1035156e-5f;  // 2^-14
+  const float ta = fmaxf(0.f, a - eps), tb = fminf(1.f, a + h + eps);
+  const float tm = 0.5f * (ta + tb), hh = 0.5f * (tb - ta);
+  return kFV ? fv_piece_reject32(x1, x2, x3, v1, v2, v3, tm, hh) : ee_piece_reject32(x1, x2, x3, v1, v2, v3, tm, hh);
+}
+
 // The test (face-vertex when kFV, else edge-edge) rejects at whatever t
 // FindCoplanerInterp returns for x_i, v_i (i = 1, 2, 3).
 template <bool kFV>
@@ -251,8 +276,9 @@ CS_HD bool ccd_pieces32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<doubl
                         V3<double> v3d) {
   const RV x1 = rv(x1d), x2 = rv(x2d), x3 = rv(x3d), v1 = rv(v1d), v2 = rv(v2d), v3 = rv(v3d);
   // the cubic k0 + k1 t + k2 t^2 + k3 t^3 of FindCoplanerInterp (triple
-  // products a . (b x c)), and the magnitude of its terms (the reference's FP64
-  // rounding of the coefficients and of each evaluation stays below 4e-15 of it)
+  // products a . (b x c)), and the magnitude of its terms: the reference's FP64
+  // rounding of the coefficients and of each evaluation stays below 4e-15 of
+  // it, and F below allows 1e-14
   R32 k[4];
   float mk = 0.f;
   {
@@ -279,26 +305,32 @@ CS_HD bool ccd_pieces32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<doubl
     for (int d = 0; d < 4; d++) k[d] = acc[d];
   }
   const float F = 1.0e-14f * mk + 1e-30f;
-  const R32 third = rc(0.33333334f, 1.0e-8f), two_thirds = rc(0.6666667f, 3.0e-8f);
   // a coefficient that may be exactly 0 in FP64 at t = 0 sends the bisection to
-  // t = 1 - 2^-15: the last piece is then tested as well
+  // t = 1 - 2^-15: the piece that ends at 1 is then tested as well
   const bool k0_zero = !(lo32(k[0]) > F || hi32(k[0]) < -F);
-  const float eps = 6.1035156e-5f;  // 2^-14
+  // pieces of 1/8, halved down to 1/32 where a piece that may hold t fails:
+  // each eighth is a tree of 7 nodes in preorder (0: the eighth; 1, 4: its
+  // halves; 2, 3 and 5, 6: their halves), a node tested only if its parent
+  // failed, and a failing leaf ends the certificate (one call site, so the
+  // piece certificate is compiled once)
+#pragma unroll 1
   for (int j = 0; j < 8; j++) {
-    const float a = 0.125f * (float)j, h = 0.125f;
-    // Bernstein coefficients of the cubic on [a, a + h]
-    const R32 K0 = k[0] + a * (k[1] + a * (k[2] + a * k[3]));
-    const R32 K1 = h * (k[1] + a * (2.f * k[2] + (3.f * a) * k[3]));
-    const R32 K2 = (h * h) * (k[2] + (3.f * a) * k[3]);
-    const R32 K3 = (h * h * h) * k[3];
-    const R32 B1 = K0 + third * K1, B2 = (K0 + two_thirds * K1) + third * K2, B3 = ((K0 + K1) + K2) + K3;
-    const bool pos = lo32(K0) > F && lo32(B1) > F && lo32(B2) > F && lo32(B3) > F;
-    const bool neg = hi32(K0) < -F && hi32(B1) < -F && hi32(B2) < -F && hi32(B3) < -F;
-    if ((pos || neg) && !(k0_zero && j == 7)) continue;  // no sign change of the FP64 cubic here
-    const float ta = fmaxf(0.f, a - eps), tb = fminf(1.f, a + h + eps);
-    const float tm = 0.5f * (ta + tb), hh = 0.5f * (tb - ta);
-    if (kFV ? !fv_piece_reject32(x1, x2, x3, v1, v2, v3, tm, hh) : !ee_piece_reject32(x1, x2, x3, v1, v2, v3, tm, hh))
-      return false;
+    unsigned need = 1u;
+#pragma unroll 1
+    for (int n = 0; n < 7; n++) {
+      if (!((need >> n) & 1u)) continue;
+      const float off = n == 3 ? 0.03125f : (n == 4 || n == 5) ? 0.0625f : n == 6 ? 0.09375f : 0.f;
+      const float h = n == 0 ? 0.125f : (n == 1 || n == 4) ? 0.0625f : 0.03125f;
+      if (piece_clear<kFV>(k, F, k0_zero, 0.125f * (float)j + off, h, x1, x2, x3, v1, v2, v3)) continue;
+      if (n == 0)
+        need |= (1u << 1) | (1u << 4);
+      else if (n == 1)
+        need |= (1u << 2) | (1u << 3);
+      else if (n == 4)
+        need |= (1u << 5) | (1u << 6);
+      else
+        return false;
+    }
   }
   return true;
 }
