@@ -204,6 +204,8 @@ CS_HD bool fv_piece_reject32(const RV& x1, const RV& x2, const RV& x3, const RV&
 //   branch), so the segments' convex hulls over the piece being more than
 //   1e-2 + 1e-6 apart along one axis, with both edges at least 1e-3 m long
 //   throughout, rejects as well.
+CS_HD bool ee_hull_far32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3,
+                         float tm, float hh);
 CS_HD bool ee_piece_reject32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3,
                              float tm, float hh) {
   const RV vp = rvpiece(x1, v1, tm, hh), W = rvpiece(x2, v2, tm, hh), Q1 = rvpiece(x3, v3, tm, hh);
@@ -222,7 +224,15 @@ CS_HD bool ee_piece_reject32(const RV& x1, const RV& x2, const RV& x3, const RV&
     const float need = 1e-2f + 1e-7f;
     if (0.9999f * (a * a) > 1.0001f * (need * need) * hi32(n2)) return true;
   }
-  // hull separation
+  return ee_hull_far32(x1, x2, x3, v1, v2, v3, tm, hh);
+}
+
+// The hull certificate of ee_piece_reject32 on its own (the piece [tm - hh,
+// tm + hh]; the whole motion for tm = hh = 1/2).
+CS_HD bool ee_hull_far32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3,
+                         float tm, float hh) {
+  const RV vp = rvpiece(x1, v1, tm, hh), W = rvpiece(x2, v2, tm, hh), Q1 = rvpiece(x3, v3, tm, hh);
+  const RV vq = Q1 - W;
   if (!(rlen2_lo(vp) > 1.0001e-6f) || !(rlen2_lo(vq) > 1.0001e-6f)) return false;
   float d[3];
   {
@@ -251,9 +261,9 @@ CS_HD bool ee_piece_reject32(const RV& x1, const RV& x2, const RV& x3, const RV&
 // elsewhere, unless the piece ends at 1 and k0 may vanish; otherwise the
 // piece, widened by 2^-14 on each side, passes the face-vertex or edge-edge
 // certificate.
-template <bool kFV>
-CS_HD bool piece_clear(const R32 k[4], float F, bool k0_zero, float a, float h, const RV& x1, const RV& x2,
-                       const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
+// The cubic k keeps one sign on [a, a + h] (a, h exact) beyond F: its
+// Bernstein coefficients there do.
+CS_HD bool cubic_one_sign(const R32 k[4], float F, float a, float h) {
   const R32 third = rc(0.33333334f, 1.0e-8f), two_thirds = rc(0.6666667f, 3.0e-8f);
   const R32 K0 = k[0] + a * (k[1] + a * (k[2] + a * k[3]));
   const R32 K1 = h * (k[1] + a * (2.f * k[2] + (3.f * a) * k[3]));
@@ -262,7 +272,13 @@ CS_HD bool piece_clear(const R32 k[4], float F, bool k0_zero, float a, float h, 
   const R32 B1 = K0 + third * K1, B2 = (K0 + two_thirds * K1) + third * K2, B3 = ((K0 + K1) + K2) + K3;
   const bool pos = lo32(K0) > F && lo32(B1) > F && lo32(B2) > F && lo32(B3) > F;
   const bool neg = hi32(K0) < -F && hi32(B1) < -F && hi32(B2) < -F && hi32(B3) < -F;
-  if ((pos || neg) && !(k0_zero && a + h == 1.f)) return true;
+  return pos || neg;
+}
+
+template <bool kFV>
+CS_HD bool piece_clear(const R32 k[4], float F, bool k0_zero, float a, float h, const RV& x1, const RV& x2,
+                       const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
+  if (cubic_one_sign(k, F, a, h) && !(k0_zero && a + h == 1.f)) return true;
   const float eps = 6.1035156e-5f;  // 2^-14
   const float ta = fmaxf(0.f, a - eps), tb = fminf(1.f, a + h + eps);
   const float tm = 0.5f * (ta + tb), hh = 0.5f * (tb - ta);
@@ -272,9 +288,7 @@ CS_HD bool piece_clear(const R32 k[4], float F, bool k0_zero, float a, float h, 
 // The test (face-vertex when kFV, else edge-edge) rejects at whatever t
 // FindCoplanerInterp returns for x_i, v_i (i = 1, 2, 3).
 template <bool kFV>
-CS_HD bool ccd_pieces32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<double> v1d, V3<double> v2d,
-                        V3<double> v3d) {
-  const RV x1 = rv(x1d), x2 = rv(x2d), x3 = rv(x3d), v1 = rv(v1d), v2 = rv(v2d), v3 = rv(v3d);
+CS_HD bool ccd_pieces32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
   // the cubic k0 + k1 t + k2 t^2 + k3 t^3 of FindCoplanerInterp (triple
   // products a . (b x c)), and the magnitude of its terms: the reference's FP64
   // rounding of the coefficients and of each evaluation stays below 4e-15 of
@@ -308,6 +322,10 @@ CS_HD bool ccd_pieces32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<doubl
   // a coefficient that may be exactly 0 in FP64 at t = 0 sends the bisection to
   // t = 1 - 2^-15: the piece that ends at 1 is then tested as well
   const bool k0_zero = !(lo32(k[0]) > F || hi32(k[0]) < -F);
+  // no sign change on all of [0, 1]: FindCoplanerInterp returns -1
+  if (!k0_zero && cubic_one_sign(k, F, 0.f, 1.f)) return true;
+  // edge-edge: the edges' hulls over the whole motion more than 1e-2 apart
+  if (!kFV && ee_hull_far32(x1, x2, x3, v1, v2, v3, 0.5f, 0.5f)) return true;
   // pieces of 1/8, halved down to 1/32 where a piece that may hold t fails:
   // each eighth is a tree of 7 nodes in preorder (0: the eighth; 1, 4: its
   // halves; 2, 3 and 5, 6: their halves), a node tested only if its parent
@@ -335,12 +353,42 @@ CS_HD bool ccd_pieces32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<doubl
   return true;
 }
 
-CS_HD bool fv_ccd_pieces32(V3<double> x1, V3<double> x2, V3<double> x3, V3<double> v1, V3<double> v2,
-                           V3<double> v3) {
+
+// True when IsContact_FV_CCD certainly rejects the face p0 p1 p2 and the vertex
+// p3 moving to q0..q3, from the differences FindCoplanerInterp forms
+// (x_i = p_i - p0, v_i = (q_i - q0) - x_i, FP64): the vertex stays on one side
+// of the start face plane (the test's sign block, bvh_aabb.cpp:683-690: the
+// four heights (p0 - p3).n, (q0 - q3).n, (q1 - q3).n, (q2 - q3).n with
+// n = x1 x2, each beyond twice its bound, which also covers the reference's FP64
+// rounding, and 1e-30, so that its products keep their signs), the four points
+// are never coplanar in [0, 1], or at any coplanarity time the vertex projects
+// outside the face.
+CS_HD bool fv_ccd_cert32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<double> v1d, V3<double> v2d,
+                         V3<double> v3d) {
+  const RV x1 = rv(x1d), x2 = rv(x2d), x3 = rv(x3d), v1 = rv(v1d), v2 = rv(v2d), v3 = rv(v3d);
+  {
+    const RV n = rcross(x1, x2);
+    const RV e3 = x3 + v3;  // q3 - q0
+    const R32 h[4] = {-rdot(x3, n), -rdot(e3, n), rdot((x1 + v1) - e3, n), rdot((x2 + v2) - e3, n)};
+    bool pos = true, neg = true;
+    for (int i = 0; i < 4; i++) {
+      const R32 w = rc(h[i].m, 2.f * h[i].r);
+      pos = pos && lo32(w) > 1e-30f;
+      neg = neg && hi32(w) < -1e-30f;
+    }
+    if (pos || neg) return true;
+  }
   return ccd_pieces32<true>(x1, x2, x3, v1, v2, v3);
 }
-CS_HD bool ee_ccd_pieces32(V3<double> x1, V3<double> x2, V3<double> x3, V3<double> v1, V3<double> v2,
-                           V3<double> v3) {
+
+// True when IsContact_EE_CCD certainly rejects the edges p0 p1 and q0 q1 moving
+// to their end points, from x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0 and their
+// changes v_i (FP64, as FindCoplanerInterp forms them): no coplanarity in
+// [0, 1], the edges more than 1e-2 apart over the whole motion, or at any
+// coplanarity time a ratio out of range or the edges apart.
+CS_HD bool ee_ccd_cert32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<double> v1d, V3<double> v2d,
+                         V3<double> v3d) {
+  const RV x1 = rv(x1d), x2 = rv(x2d), x3 = rv(x3d), v1 = rv(v1d), v2 = rv(v2d), v3 = rv(v3d);
   return ccd_pieces32<false>(x1, x2, x3, v1, v2, v3);
 }
 

@@ -274,137 +274,9 @@ CS_HD double coplanar_time(V3<double> s0, V3<double> s1, V3<double> s2, V3<doubl
   return bisect_cubic(r0, r1, f0, k0, k1, k2, k3);
 }
 
-// FP32 vector with a bound on each component's error
-struct F3E {
-  float v[3], e[3];
-};
-
-__device__ __forceinline__ F3E f3e_cross(const F3E& a, const F3E& b) {
-  const float u = 5.9604645e-8f;
-  F3E c;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const int i = (k + 1) % 3, j = (k + 2) % 3;
-    const float m1 = a.v[i] * b.v[j], m2 = a.v[j] * b.v[i];
-    c.v[k] = m1 - m2;
-    c.e[k] = 1.001f * ((fabsf(a.v[i]) + a.e[i]) * b.e[j] + fabsf(b.v[j]) * a.e[i] +
-                       (fabsf(a.v[j]) + a.e[j]) * b.e[i] + fabsf(b.v[i]) * a.e[j] +
-                       2.1f * u * (fabsf(m1) + fabsf(m2)));
-  }
-  return c;
-}
-
-// a . (b x c) with its error bound and the sum of the magnitudes of its terms
-__device__ __forceinline__ void f3e_stp(const F3E& a, const F3E& b, const F3E& c, float& t, float& e, float& m) {
-  const float u = 5.9604645e-8f;
-  const F3E x = f3e_cross(b, c);
-  float s = 0.f, r = 0.f, mm = 0.f;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const float p = a.v[k] * x.v[k];
-    s = s + p;
-    r += (fabsf(a.v[k]) + a.e[k]) * x.e[k] + fabsf(x.v[k]) * a.e[k];
-    mm += fabsf(a.v[k]) * (fabsf(b.v[(k + 1) % 3] * c.v[(k + 2) % 3]) + fabsf(b.v[(k + 2) % 3] * c.v[(k + 1) % 3]));
-  }
-  t = s;
-  e = 1.001f * (r + 3.1f * u * mm);
-  m = mm;
-}
-
-__device__ __forceinline__ F3E f3e_round(V3<double> d) {
-  F3E r;
-  r.v[0] = (float)d.x;
-  r.v[1] = (float)d.y;
-  r.v[2] = (float)d.z;
-#pragma unroll
-  for (int k = 0; k < 3; k++) r.e[k] = 5.97e-8f * fabsf(r.v[k]);  // round to nearest: 2^-24 relative
-  return r;
-}
-
-// True when FindCoplanerInterp (coplanar_time) certainly returns -1 for the
-// vectors it forms from the start positions and displacements: x_i = s_i - s0,
-// v_i = (e_i - e0) - x_i, computed in FP64 exactly as it does and passed here.
-// The cubic k0 + k1 t + k2 t^2 + k3 t^3 (k from the triple products) has its
-// Bernstein coefficients on [0, 1] evaluated in FP32 with error bounds; when
-// all four keep one sign with twice their bound to spare (which also covers the
-// FP64 rounding of the coefficients and of the cubic's evaluations), the cubic
-// keeps that sign on [0, 1], no evaluation the root finder makes changes sign,
-// and it returns -1.
-__device__ __forceinline__ bool ccd_no_root32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<double> v1d,
-                                              V3<double> v2d, V3<double> v3d) {
-  const float u = 5.9604645e-8f;
-  const F3E x1 = f3e_round(x1d), x2 = f3e_round(x2d), x3 = f3e_round(x3d);
-  const F3E v1 = f3e_round(v1d), v2 = f3e_round(v2d), v3 = f3e_round(v3d);
-  float t[8], e[8], m[8];
-  f3e_stp(x3, x1, x2, t[0], e[0], m[0]);  // k0
-  f3e_stp(v3, x1, x2, t[1], e[1], m[1]);  // k1
-  f3e_stp(x3, v1, x2, t[2], e[2], m[2]);
-  f3e_stp(x3, x1, v2, t[3], e[3], m[3]);
-  f3e_stp(v3, v1, x2, t[4], e[4], m[4]);  // k2
-  f3e_stp(v3, x1, v2, t[5], e[5], m[5]);
-  f3e_stp(x3, v1, v2, t[6], e[6], m[6]);
-  f3e_stp(v3, v1, v2, t[7], e[7], m[7]);  // k3
-  const float k0 = t[0], k1 = (t[1] + t[2]) + t[3], k2 = (t[4] + t[5]) + t[6], k3 = t[7];
-  const float mk = m[0] + m[1] + m[2] + m[3] + m[4] + m[5] + m[6] + m[7];
-  const float ek0 = e[0], ek1 = 1.001f * (e[1] + e[2] + e[3] + 2.1f * u * (fabsf(t[1]) + fabsf(t[2]) + fabsf(t[3]))),
-              ek2 = 1.001f * (e[4] + e[5] + e[6] + 2.1f * u * (fabsf(t[4]) + fabsf(t[5]) + fabsf(t[6]))),
-              ek3 = e[7];
-  // FP64 rounding of the reference's coefficients and cubic evaluations
-  const float f64 = 4.0e-15f * mk;
-  // Bernstein coefficients of the cubic on [0, 1]
-  const float b0 = k0, b1 = k0 + k1 * (1.0f / 3.0f), b2 = k0 + k1 * (2.0f / 3.0f) + k2 * (1.0f / 3.0f),
-              b3 = ((k0 + k1) + k2) + k3;
-  const float eb0 = ek0, eb1 = 1.001f * (ek0 + ek1 * 0.34f + 2.0f * u * (fabsf(k0) + fabsf(k1))),
-              eb2 = 1.001f * (ek0 + ek1 * 0.67f + ek2 * 0.34f + 3.0f * u * (fabsf(k0) + fabsf(k1) + fabsf(k2))),
-              eb3 = 1.001f * (ek0 + ek1 + ek2 + ek3 + 3.1f * u * (fabsf(k0) + fabsf(k1) + fabsf(k2) + fabsf(k3)));
-  const bool pos = b0 - 2.0f * eb0 > f64 && b1 - 2.0f * eb1 > f64 && b2 - 2.0f * eb2 > f64 && b3 - 2.0f * eb3 > f64;
-  const bool neg = b0 + 2.0f * eb0 < -f64 && b1 + 2.0f * eb1 < -f64 && b2 + 2.0f * eb2 < -f64 &&
-                   b3 + 2.0f * eb3 < -f64;
-  return pos || neg;
-}
-
-// a . b with its error bound, for FP32 vectors with per-component error bounds
-__device__ __forceinline__ void f3e_dot(const F3E& a, const F3E& b, float& t, float& e) {
-  const float u = 5.9604645e-8f;
-  float s = 0.f, r = 0.f, mm = 0.f;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    const float p = a.v[k] * b.v[k];
-    s = s + p;
-    r += (fabsf(a.v[k]) + a.e[k]) * b.e[k] + fabsf(b.v[k]) * a.e[k];
-    mm += fabsf(p);
-  }
-  t = s;
-  e = 1.001f * (r + 3.1f * u * mm);
-}
-
-// True when the coplanarity-sign rejection of IsContact_FV_CCD
-// (bvh_aabb.cpp:683-690, the first block of fv_ccd) certainly fires: with the
-// start normal n = (p1 - p0) x (p2 - p0), the four signed heights
-// (p0 - p3).n, (q0 - q3).n, (q1 - q3).n, (q2 - q3).n have one sign.  The
-// differences arrive as FP64 values (rounded here to FP32, 2^-24 relative);
-// every product and sum carries an error bound, and each height must clear
-// twice its bound (which covers the FP64 evaluation's own rounding) and a floor
-// of 1e-30, so the FP64 products t0 * ti are nonzero with the same sign.
-__device__ __forceinline__ bool fv_sign_reject32(V3<double> e1, V3<double> e2, V3<double> h0, V3<double> h1,
-                                                 V3<double> h2, V3<double> h3) {
-  const F3E n = f3e_cross(f3e_round(e1), f3e_round(e2));
-  float t[4], e[4];
-  f3e_dot(f3e_round(h0), n, t[0], e[0]);
-  f3e_dot(f3e_round(h1), n, t[1], e[1]);
-  f3e_dot(f3e_round(h2), n, t[2], e[2]);
-  f3e_dot(f3e_round(h3), n, t[3], e[3]);
-  bool pos = true, neg = true;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    pos = pos && t[k] - 2.0f * e[k] > 1.0e-30f;
-    neg = neg && t[k] + 2.0f * e[k] < -1.0e-30f;
-  }
-  return pos || neg;
-}
-
 // Closest points of segments a0 a1 and b0 b1 (FP32, clamped): the vector from
-// the point on a to the point on b.  Only a direction for the certificate below.
+// the point on a to the point on b.  Only a direction for the hull certificate
+// of the continuous-collision tests (cert.cuh).
 CS_HD void seg_seg_dir32(const float a0[3], const float a1[3], const float b0[3],
                                               const float b1[3], float d[3]) {
   float u[3], v[3], w[3];
@@ -430,75 +302,6 @@ CS_HD void seg_seg_dir32(const float a0[3], const float a1[3], const float b0[3]
   }
 #pragma unroll
   for (int k = 0; k < 3; k++) d[k] = (b0[k] + sb * v[k]) - (a0[k] + sa * u[k]);
-}
-
-// True when IsContact_EE_CCD's distance test (bvh_aabb.cpp:786-791: the edges'
-// distance at the coplanarity time must not exceed 1e-2) certainly rejects,
-// for edges p (p0, p1) and q (q0, q1) moving from s to e.  At every time in
-// [0, 1] an edge lies in the convex hull of its four start and end points, so
-// a separating axis d along which the two hulls are more than dmax apart bounds
-// the distance the reference computes there from below: its closest points lie
-// on the segments whenever both ratios pass, and its parallel-edge branch
-// (|vp x vq| < 1e-10) measures a line distance that undercuts the segment
-// distance by at most 1e-10 over the length of an edge.  The certificate
-// therefore requires both edges to be at least 1e-3 m long at the start and the
-// end without turning over (start and end directions with a positive dot
-// product, so no edge degenerates in between) and keeps a margin of 1e-6 m,
-// which also covers the FP64 rounding of the reference's interpolation and
-// distance.  The points enter as FP64 differences from p0s rounded to FP32, and
-// each projection carries an error bound.
-__device__ __forceinline__ bool ee_ccd_far32(V3<double> p0s, V3<double> p1s, V3<double> q0s, V3<double> q1s,
-                                             V3<double> p0e, V3<double> p1e, V3<double> q0e, V3<double> q1e,
-                                             double dmax) {
-  {
-    // edge vectors at the start and the end (FP64 differences, rounded)
-    const F3E es[2] = {f3e_round(p1s - p0s), f3e_round(q1s - q0s)};
-    const F3E ee[2] = {f3e_round(p1e - p0e), f3e_round(q1e - q0e)};
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const float ls = es[k].v[0] * es[k].v[0] + es[k].v[1] * es[k].v[1] + es[k].v[2] * es[k].v[2];
-      const float le = ee[k].v[0] * ee[k].v[0] + ee[k].v[1] * ee[k].v[1] + ee[k].v[2] * ee[k].v[2];
-      const float se = es[k].v[0] * ee[k].v[0] + es[k].v[1] * ee[k].v[1] + es[k].v[2] * ee[k].v[2];
-      // 1.1e-6: (1e-3 m)^2 with room for the rounding of these sums
-      if (!(ls > 1.1e-6f) || !(le > 1.1e-6f) || !(se > 1.0e-3f * sqrtf(ls * le))) return false;
-    }
-  }
-  const F3E P[4] = {f3e_round(p0s - p0s), f3e_round(p1s - p0s), f3e_round(p0e - p0s), f3e_round(p1e - p0s)};
-  const F3E Q[4] = {f3e_round(q0s - p0s), f3e_round(q1s - p0s), f3e_round(q0e - p0s), f3e_round(q1e - p0s)};
-  // direction: closest points of the edges halfway through the motion
-  float a0[3], a1[3], b0[3], b1[3], d[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    a0[k] = 0.5f * (P[0].v[k] + P[2].v[k]);
-    a1[k] = 0.5f * (P[1].v[k] + P[3].v[k]);
-    b0[k] = 0.5f * (Q[0].v[k] + Q[2].v[k]);
-    b1[k] = 0.5f * (Q[1].v[k] + Q[3].v[k]);
-  }
-  seg_seg_dir32(a0, a1, b0, b1, d);
-  const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-  if (!(dd > 0.f) || !isfinite(dd)) return false;
-  F3E dv;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    dv.v[k] = d[k];
-    dv.e[k] = 0.f;  // any axis will do: d is taken as exact
-  }
-  float pmax = -INFINITY, pmin = INFINITY, qmax = -INFINITY, qmin = INFINITY;
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    float t, e;
-    f3e_dot(P[m], dv, t, e);
-    pmax = fmaxf(pmax, t + e);
-    pmin = fminf(pmin, t - e);
-    f3e_dot(Q[m], dv, t, e);
-    qmax = fmaxf(qmax, t + e);
-    qmin = fminf(qmin, t - e);
-  }
-  // |d| from above, and the gap from below (each subtraction rounded down)
-  const float dlen = __fmul_ru(__fsqrt_ru(dd), 1.0000005f);
-  const float need = __fmul_ru(__double2float_ru(dmax + 1.0e-6), dlen);
-  const float gap = fmaxf(__fsub_rd(qmin, pmax), __fsub_rd(pmin, qmax));
-  return gap > need;
 }
 
 // ---------------------------------------------------------------------------

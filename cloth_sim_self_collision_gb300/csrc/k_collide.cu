@@ -484,17 +484,14 @@ __device__ __forceinline__ void narrow_fv_body(const Arena& A, const ContactBufs
     } else {
       const V3<double> q0 = end_pos(xs, vs, f0, P.dt), q1 = end_pos(xs, vs, f1, P.dt);
       const V3<double> q2 = end_pos(xs, vs, f2, P.dt), q3 = end_pos(xs, vs, q, P.dt);
-      // FP32 certificates that the FP64 test rejects: the vertex stays on one
-      // side of the start face plane (the test's sign block), the four points
-      // are never coplanar in [0, 1] (FindCoplanerInterp returns -1), or at any
-      // coplanarity time the vertex projects outside the face (cert.cuh); all
+      // FP32 certificates that the FP64 test rejects (cert.cuh): the vertex
+      // stays on one side of the start face plane (the test's sign block), the
+      // four points are never coplanar in [0, 1] (FindCoplanerInterp returns
+      // -1), or at any coplanarity time the vertex projects outside the face;
       // from the FP64 differences the FP64 test itself forms
-      const V3<double> x1 = p1 - p0, x2 = p2 - p0;
-      if (fv_sign_reject32(x1, x2, p0 - p3, q0 - q3, q1 - q3, q2 - q3)) continue;
-      const V3<double> x3 = p3 - p0;
+      const V3<double> x1 = p1 - p0, x2 = p2 - p0, x3 = p3 - p0;
       const V3<double> v1 = (q1 - q0) - x1, v2 = (q2 - q0) - x2, v3 = (q3 - q0) - x3;
-      if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
-      if (fv_ccd_pieces32(x1, x2, x3, v1, v2, v3)) continue;
+      if (fv_ccd_cert32(x1, x2, x3, v1, v2, v3)) continue;
       // left to the FP64 test (k_narrow_fv64), in a packed queue
       C.queue64[0][warp_append(&C.counters[10])] = it;
     }
@@ -559,14 +556,13 @@ __device__ __forceinline__ void narrow_ee_body(const Arena& A, const ContactBufs
     } else {
       const V3<double> p0e = end_pos(xs, vs, i0, P.dt), p1e = end_pos(xs, vs, i1, P.dt);
       const V3<double> q0e = end_pos(xs, vs, j0, P.dt), q1e = end_pos(xs, vs, j1, P.dt);
-      // no coplanarity in [0, 1]: the vectors coplanar_time forms, in FP64 as it does
+      // FP32 certificates that the FP64 test rejects (cert.cuh): no coplanarity
+      // in [0, 1], the edges more than the test's 1e-2 apart over the whole
+      // motion, or at any coplanarity time a ratio out of range or the edges
+      // apart; from the vectors coplanar_time forms, in FP64 as it does
       const V3<double> x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0;
       const V3<double> v1 = (p1e - p0e) - x1, v2 = (q0e - p0e) - x2, v3 = (q1e - p0e) - x3;
-      if (ccd_no_root32(x1, x2, x3, v1, v2, v3)) continue;
-      // the edges stay more than the test's 1e-2 apart over the whole motion
-      if (ee_ccd_far32(p0, p1, q0, q1, p0e, p1e, q0e, q1e, 1.0e-2)) continue;
-      // at any coplanarity time a ratio is out of range or the edges are apart
-      if (ee_ccd_pieces32(x1, x2, x3, v1, v2, v3)) continue;
+      if (ee_ccd_cert32(x1, x2, x3, v1, v2, v3)) continue;
       C.queue64[1][warp_append(&C.counters[11])] = it;
     }
   }

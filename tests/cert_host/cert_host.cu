@@ -24,7 +24,7 @@ extern "C" void cert_fv_batch(int n, const double* p, int* out) {
   for (int i = 0; i < n; i++) {
     V3<double> x[3], v[3];
     diffs(p + 24 * (size_t)i, x, v);
-    out[i] = cs::fv_ccd_pieces32(x[0], x[1], x[2], v[0], v[1], v[2]);
+    out[i] = cs::fv_ccd_cert32(x[0], x[1], x[2], v[0], v[1], v[2]);
   }
 }
 
@@ -32,6 +32,6 @@ extern "C" void cert_ee_batch(int n, const double* p, int* out) {
   for (int i = 0; i < n; i++) {
     V3<double> x[3], v[3];
     diffs(p + 24 * (size_t)i, x, v);
-    out[i] = cs::ee_ccd_pieces32(x[0], x[1], x[2], v[0], v[1], v[2]);
+    out[i] = cs::ee_ccd_cert32(x[0], x[1], x[2], v[0], v[1], v[2]);
   }
 }
