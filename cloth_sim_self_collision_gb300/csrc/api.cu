@@ -993,6 +993,8 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_MX_CAP")) c->mx_cap = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_TAIL_SLICES")) c->mx_tail_slices = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_NARROW_REGS")) c->narrow_regs = std::atoi(e) == 128 ? 128 : 0;
+  // contexts made by the library itself (the serving loop) take the frame mode from here
+  if (const char* e = std::getenv("CLOTHGPU_FRAME_MODE")) c->graph_mode = std::strcmp(e, "host") != 0;
   c->A.narrow_regs = c->narrow_regs;
   *out = c;
   return CS_OK;
