@@ -299,6 +299,7 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
   A.vb32 = m.alloc<float>(6 * (size_t)NV);
   A.edge_uv = m.upload(edge_uv, s);
   A.vdirty = m.alloc<int>(NV);
+  A.ccd32 = m.alloc<float4>(3 * (size_t)NV);
   A.tdirty = m.alloc<int>(NT);
   CK(cudaMemsetAsync(A.tdirty, 0, sizeof(int) * (size_t)std::max(NT, 1), s));
   A.uf = m.alloc<int>(NV);
@@ -950,6 +951,7 @@ size_t cloth_device_bytes(const ClothTopo& t) {
   // and the candidate buffers
   b += (16 * nt + 4096) * 8 * 6 + (4 * nt + 4096) * 120;
   b += np * (2 * 4 + 2 * 8 + 72);              // vertex marks, zone keys and sums
+  b += np * 48;                                // FP32 hi/lo positions and displacements
   return b + (1 << 16);
 }
 

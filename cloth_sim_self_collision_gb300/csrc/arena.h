@@ -128,6 +128,10 @@ struct Arena {
   // incremental CCD re-detection: vertices / triangles whose velocity changed
   // since the last detection
   int *vdirty = nullptr, *tdirty = nullptr;
+  // per vertex, for the continuous-collision certificates of a detection: the
+  // start position and the displacement over the frame as FP32 hi/lo parts
+  // (cert.cuh PS, three float4)
+  float4* ccd32 = nullptr;
   // mixed precision: FP32 copy of the matrix in warp slices (SELL-32: 32 rows per
   // slice, blocks of a slice stored entry-major so every load is 32 consecutive
   // floats), block-Jacobi inverse, FP32 work vectors

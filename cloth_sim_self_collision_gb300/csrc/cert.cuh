@@ -155,6 +155,38 @@ CS_HD RV rvpiece(const RV& x, const RV& d, float tm, float hh) {
   return c;
 }
 
+// A point's start position p and its displacement d = e - p over the frame
+// (e its end position, d formed in FP64), each coordinate as FP32 hi + lo
+// parts (hi the FP64 value rounded, lo the remainder rounded; hi + lo is within
+// 2^-48 of the value): 12 floats, three float4 in memory.
+struct PS {
+  float ph[3], pl[3], dh[3], dl[3];
+};
+
+// b - a of two hi/lo values: the parts subtracted apart, then added; the bound
+// takes each rounding and the splits' own error
+CS_HD R32 hl_diff(float ah, float al, float bh, float bl) {
+  const float dh = bh - ah, dl = bl - al;
+  R32 c;
+  c.m = dh + dl;
+  c.r = 1.001f * (kU24 * (fabsf(dh) + fabsf(dl) + fabsf(c.m)) + 4e-15f * (fabsf(ah) + fabsf(bh))) + 1e-37f;
+  return c;
+}
+// x = p_b - p_a and v = d_b - d_a: the differences FindCoplanerInterp forms
+// (x = p_b - p_a, v = (e_b - e_a) - x, in FP64), enclosed: v's bound adds the
+// FP64 roundings that separate the reference's v from d_b - d_a (its own two
+// subtractions and those of d), 4e-16 of the magnitudes involved
+CS_HD void hl_xv1(const PS& a, const PS& b, int k, R32& x, R32& v) {
+  x = hl_diff(a.ph[k], a.pl[k], b.ph[k], b.pl[k]);
+  v = hl_diff(a.dh[k], a.dl[k], b.dh[k], b.dl[k]);
+  v.r = 1.001f * (v.r + 4e-16f * (fabsf(x.m) + fabsf(v.m) + fabsf(a.dh[k]) + fabsf(b.dh[k]))) + 1e-37f;
+}
+CS_HD void hl_xv(const PS& a, const PS& b, RV& x, RV& v) {
+  hl_xv1(a, b, 0, x.x, v.x);
+  hl_xv1(a, b, 1, x.y, v.y);
+  hl_xv1(a, b, 2, x.z, v.z);
+}
+
 // a ratio N / D of the reference (D > 0) certainly outside [0, 1], with margin M
 CS_HD bool ratio_out(R32 N, R32 D, float M) { return hi32(N) < -M || lo32(N - D) > M; }
 
@@ -355,17 +387,15 @@ CS_HD bool ccd_pieces32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, 
 
 
 // True when IsContact_FV_CCD certainly rejects the face p0 p1 p2 and the vertex
-// p3 moving to q0..q3, from the differences FindCoplanerInterp forms
-// (x_i = p_i - p0, v_i = (q_i - q0) - x_i, FP64): the vertex stays on one side
+// p3 moving to q0..q3, from enclosures of the differences FindCoplanerInterp
+// forms (x_i = p_i - p0, v_i = (q_i - q0) - x_i): the vertex stays on one side
 // of the start face plane (the test's sign block, bvh_aabb.cpp:683-690: the
 // four heights (p0 - p3).n, (q0 - q3).n, (q1 - q3).n, (q2 - q3).n with
 // n = x1 x2, each beyond twice its bound, which also covers the reference's FP64
 // rounding, and 1e-30, so that its products keep their signs), the four points
 // are never coplanar in [0, 1], or at any coplanarity time the vertex projects
 // outside the face.
-CS_HD bool fv_ccd_cert32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<double> v1d, V3<double> v2d,
-                         V3<double> v3d) {
-  const RV x1 = rv(x1d), x2 = rv(x2d), x3 = rv(x3d), v1 = rv(v1d), v2 = rv(v2d), v3 = rv(v3d);
+CS_HD bool fv_ccd_cert32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
   {
     const RV n = rcross(x1, x2);
     const RV e3 = x3 + v3;  // q3 - q0
@@ -380,16 +410,30 @@ CS_HD bool fv_ccd_cert32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<doub
   }
   return ccd_pieces32<true>(x1, x2, x3, v1, v2, v3);
 }
+// the same from the points' hi/lo parts (face p0 p1 p2, vertex p3)
+CS_HD bool fv_ccd_cert32(const PS& s0, const PS& s1, const PS& s2, const PS& s3) {
+  RV x1, x2, x3, v1, v2, v3;
+  hl_xv(s0, s1, x1, v1);
+  hl_xv(s0, s2, x2, v2);
+  hl_xv(s0, s3, x3, v3);
+  return fv_ccd_cert32(x1, x2, x3, v1, v2, v3);
+}
 
 // True when IsContact_EE_CCD certainly rejects the edges p0 p1 and q0 q1 moving
-// to their end points, from x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0 and their
-// changes v_i (FP64, as FindCoplanerInterp forms them): no coplanarity in
+// to their end points, from enclosures of x1 = p1 - p0, x2 = q0 - p0,
+// x3 = q1 - p0 and their changes v_i (as FindCoplanerInterp forms them): no coplanarity in
 // [0, 1], the edges more than 1e-2 apart over the whole motion, or at any
 // coplanarity time a ratio out of range or the edges apart.
-CS_HD bool ee_ccd_cert32(V3<double> x1d, V3<double> x2d, V3<double> x3d, V3<double> v1d, V3<double> v2d,
-                         V3<double> v3d) {
-  const RV x1 = rv(x1d), x2 = rv(x2d), x3 = rv(x3d), v1 = rv(v1d), v2 = rv(v2d), v3 = rv(v3d);
+CS_HD bool ee_ccd_cert32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
   return ccd_pieces32<false>(x1, x2, x3, v1, v2, v3);
+}
+// the same from the points' hi/lo parts (edges p0 p1 and q0 q1)
+CS_HD bool ee_ccd_cert32(const PS& p0, const PS& p1, const PS& q0, const PS& q1) {
+  RV x1, x2, x3, v1, v2, v3;
+  hl_xv(p0, p1, x1, v1);
+  hl_xv(p0, q0, x2, v2);
+  hl_xv(p0, q1, x3, v3);
+  return ee_ccd_cert32(x1, x2, x3, v1, v2, v3);
 }
 
 }  // namespace cs

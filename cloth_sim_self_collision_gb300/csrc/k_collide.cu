@@ -65,6 +65,41 @@ __device__ __forceinline__ V3<double> end_pos(const double* x, const double* v, 
   return mk<double>(x[3 * i + 0] + dt * v[3 * i + 0], x[3 * i + 1] + dt * v[3 * i + 1], x[3 * i + 2] + dt * v[3 * i + 2]);
 }
 
+// The start positions and the displacements e - x (e = end_pos, FP64) of the
+// active cloths' vertices as FP32 hi/lo parts, for the certificates of a
+// continuous-collision detection
+__global__ void k_ccd_split(Arena A, const double* xs, const double* vs) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.nv) return;
+  const int inst = A.vinst[v];
+  if (!A.active[inst]) return;
+  const V3<double> p = ld3(xs, v), e = end_pos(xs, vs, v, A.prm[inst].dt);
+  const double pv[3] = {p.x, p.y, p.z}, dv[3] = {e.x - p.x, e.y - p.y, e.z - p.z};
+  float f[12];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    f[c] = (float)pv[c];
+    f[3 + c] = (float)(pv[c] - (double)f[c]);
+    f[6 + c] = (float)dv[c];
+    f[9 + c] = (float)(dv[c] - (double)f[6 + c]);
+  }
+  float4* o = A.ccd32 + 3 * (size_t)v;
+  o[0] = make_float4(f[0], f[1], f[2], f[3]);
+  o[1] = make_float4(f[4], f[5], f[6], f[7]);
+  o[2] = make_float4(f[8], f[9], f[10], f[11]);
+}
+
+__device__ __forceinline__ PS ld_ps(const Arena& A, int v) {
+  const float4* q = A.ccd32 + 3 * (size_t)v;
+  const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+  PS s;
+  s.ph[0] = a.x, s.ph[1] = a.y, s.ph[2] = a.z;
+  s.pl[0] = a.w, s.pl[1] = b.x, s.pl[2] = b.y;
+  s.dh[0] = b.z, s.dh[1] = b.w, s.dh[2] = c.x;
+  s.dl[0] = c.y, s.dl[1] = c.z, s.dl[2] = c.w;
+  return s;
+}
+
 // BuildBoundingBoxChild_Prx / _CCD (bvh_aabb.cpp:23-106)
 __global__ void k_refit(Arena A, int ccd, const double* xs, const double* vs, double delta_override) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -482,16 +517,12 @@ __device__ __forceinline__ void narrow_fv_body(const Arena& A, const ContactBufs
       const Box bb = A.box[A.noff[inst] + (tf - A.toff[inst])];
       if (fv_proximity(f0, f1, f2, q, p0, p1, p2, p3, bb, delta)) emit(C, 1, f0, f1, f2, q, na, nb, test);
     } else {
-      const V3<double> q0 = end_pos(xs, vs, f0, P.dt), q1 = end_pos(xs, vs, f1, P.dt);
-      const V3<double> q2 = end_pos(xs, vs, f2, P.dt), q3 = end_pos(xs, vs, q, P.dt);
       // FP32 certificates that the FP64 test rejects (cert.cuh): the vertex
       // stays on one side of the start face plane (the test's sign block), the
       // four points are never coplanar in [0, 1] (FindCoplanerInterp returns
       // -1), or at any coplanarity time the vertex projects outside the face;
-      // from the FP64 differences the FP64 test itself forms
-      const V3<double> x1 = p1 - p0, x2 = p2 - p0, x3 = p3 - p0;
-      const V3<double> v1 = (q1 - q0) - x1, v2 = (q2 - q0) - x2, v3 = (q3 - q0) - x3;
-      if (fv_ccd_cert32(x1, x2, x3, v1, v2, v3)) continue;
+      // from enclosures of the FP64 differences the FP64 test itself forms
+      if (fv_ccd_cert32(ld_ps(A, f0), ld_ps(A, f1), ld_ps(A, f2), ld_ps(A, q))) continue;
       // left to the FP64 test (k_narrow_fv64), in a packed queue
       C.queue64[0][warp_append(&C.counters[10])] = it;
     }
@@ -554,15 +585,11 @@ __device__ __forceinline__ void narrow_ee_body(const Arena& A, const ContactBufs
       count_fp64_test(A, 3);
       if (ee_proximity(i0, i1, j0, j1, p0, p1, q0, q1, delta)) emit(C, 0, i0, i1, j0, j1, na, nb, test);
     } else {
-      const V3<double> p0e = end_pos(xs, vs, i0, P.dt), p1e = end_pos(xs, vs, i1, P.dt);
-      const V3<double> q0e = end_pos(xs, vs, j0, P.dt), q1e = end_pos(xs, vs, j1, P.dt);
       // FP32 certificates that the FP64 test rejects (cert.cuh): no coplanarity
       // in [0, 1], the edges more than the test's 1e-2 apart over the whole
       // motion, or at any coplanarity time a ratio out of range or the edges
-      // apart; from the vectors coplanar_time forms, in FP64 as it does
-      const V3<double> x1 = p1 - p0, x2 = q0 - p0, x3 = q1 - p0;
-      const V3<double> v1 = (p1e - p0e) - x1, v2 = (q0e - p0e) - x2, v3 = (q1e - p0e) - x3;
-      if (ee_ccd_cert32(x1, x2, x3, v1, v2, v3)) continue;
+      // apart; from enclosures of the vectors coplanar_time forms
+      if (ee_ccd_cert32(ld_ps(A, i0), ld_ps(A, i1), ld_ps(A, j0), ld_ps(A, j1))) continue;
       C.queue64[1][warp_append(&C.counters[11])] = it;
     }
   }
@@ -618,6 +645,10 @@ __global__ void __launch_bounds__(kT, 4) k_narrow_ee64_b4(Arena A, ContactBufs C
 void narrow_fp64_passes(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
                         double delta_override, int grid, cudaStream_t s) {
   const bool b4 = A.narrow_regs == 128;
+  if (ccd) {
+    k_ccd_split<<<nblk(A.nv), kT, 0, s>>>(A, xs, vs);
+    g_launches++;
+  }
   prof_begin(PK_NARROW_FV, s);
   if (b4)
     k_narrow_fv_b4<<<grid, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <condition_variable>
 #include <deque>
@@ -363,6 +364,16 @@ int cs_server_create(const cs_server_config* cfg, cs_server** out) {
   cs_ctx* ctx = nullptr;
   const int st = cs_create(cfg->device, cfg->precision, &ctx);
   if (st != CS_OK) return st;
+  // The serving arena changes at every admission and retirement, and a frame
+  // graph is captured again after each change: measured at 2 scenes/s, graph
+  // frames tripled the admission latency (the capture and instantiation on the
+  // worker thread, the builder's packing slowed beside them) and lowered the
+  // throughput.  So the worker steps host-driven frames unless
+  // CLOTHGPU_FRAME_MODE=graph asks otherwise.
+  {
+    const char* e = std::getenv("CLOTHGPU_FRAME_MODE");
+    if (!e || std::strcmp(e, "graph") != 0) cs_set_frame_mode(ctx, CS_FRAME_HOST);
+  }
   cs_server* S = new cs_server();
   S->cfg = *cfg;
   S->ctx = ctx;

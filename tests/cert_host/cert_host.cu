@@ -1,20 +1,23 @@
 // Host build of the FP32 continuous-collision certificates (cert.cuh) for the
 // CPU tests: the same float arithmetic as the device (round to nearest, no
-// contraction), with the outward-rounded bounds one ulp wider.
+// contraction), with the outward-rounded bounds one ulp wider, and the same
+// hi/lo split of positions and displacements as the device's k_ccd_split.
 #include "cert.cuh"
 
-using cs::V3;
-
 namespace {
-V3<double> pt(const double* a, int k) { return cs::mk<double>(a[3 * k], a[3 * k + 1], a[3 * k + 2]); }
-
-// x_i = p_i - p0 at the start and v_i = (e_i - e0) - x_i, as FindCoplanerInterp forms them
-void diffs(const double* a, V3<double> x[3], V3<double> v[3]) {
-  const V3<double> s0 = pt(a, 0), e0 = pt(a, 4);
-  for (int i = 0; i < 3; i++) {
-    x[i] = pt(a, 1 + i) - s0;
-    v[i] = (pt(a, 5 + i) - e0) - x[i];
+// point k of a configuration: start position p and end position e, split as
+// the device splits x and e - x
+cs::PS split(const double* a, int k) {
+  cs::PS s;
+  for (int c = 0; c < 3; c++) {
+    const double p = a[3 * k + c], e = a[12 + 3 * k + c];
+    const double d = e - p;
+    s.ph[c] = (float)p;
+    s.pl[c] = (float)(p - (double)s.ph[c]);
+    s.dh[c] = (float)d;
+    s.dl[c] = (float)(d - (double)s.dh[c]);
   }
+  return s;
 }
 }  // namespace
 
@@ -22,16 +25,14 @@ void diffs(const double* a, V3<double> x[3], V3<double> v[3]) {
 // certificate proves the reference's test rejects
 extern "C" void cert_fv_batch(int n, const double* p, int* out) {
   for (int i = 0; i < n; i++) {
-    V3<double> x[3], v[3];
-    diffs(p + 24 * (size_t)i, x, v);
-    out[i] = cs::fv_ccd_cert32(x[0], x[1], x[2], v[0], v[1], v[2]);
+    const double* a = p + 24 * (size_t)i;
+    out[i] = cs::fv_ccd_cert32(split(a, 0), split(a, 1), split(a, 2), split(a, 3));
   }
 }
 
 extern "C" void cert_ee_batch(int n, const double* p, int* out) {
   for (int i = 0; i < n; i++) {
-    V3<double> x[3], v[3];
-    diffs(p + 24 * (size_t)i, x, v);
-    out[i] = cs::ee_ccd_cert32(x[0], x[1], x[2], v[0], v[1], v[2]);
+    const double* a = p + 24 * (size_t)i;
+    out[i] = cs::ee_ccd_cert32(split(a, 0), split(a, 1), split(a, 2), split(a, 3));
   }
 }
