@@ -411,6 +411,9 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
 void install(cs_ctx* c, ArenaSet& o) {
   graph_release(c);
   o.A.narrow_regs = c->narrow_regs;
+  o.A.bar_sleep_ns = c->bar_sleep_ns;
+  o.A.bar_timeout_ns = c->bar_timeout_ns;
+  o.A.bar_hold = c->bar_hold;
   std::swap(c->A, o.A);
   std::swap(c->C, o.C);
   std::swap(c->mem, o.mem);
@@ -997,7 +1000,16 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_NARROW_REGS")) c->narrow_regs = std::atoi(e) == 128 ? 128 : 0;
   // contexts made by the library itself (the serving loop) take the frame mode from here
   if (const char* e = std::getenv("CLOTHGPU_FRAME_MODE")) c->graph_mode = std::strcmp(e, "host") != 0;
+  if (const char* e = std::getenv("CLOTHGPU_BAR_SLEEP_NS")) c->bar_sleep_ns = std::max(0, std::atoi(e));
+  // failure-detection tests: a short barrier time-out, and a barrier that
+  // block 0 never reaches (every wait then runs out and the frame fails with
+  // CS_ERR_CUDA, the context staying usable)
+  if (const char* e = std::getenv("CLOTHGPU_BAR_TIMEOUT_NS")) c->bar_timeout_ns = std::max(1000LL, std::atoll(e));
+  if (const char* e = std::getenv("CLOTHGPU_BAR_HOLD")) c->bar_hold = std::atoi(e) != 0;
   c->A.narrow_regs = c->narrow_regs;
+  c->A.bar_sleep_ns = c->bar_sleep_ns;
+  c->A.bar_timeout_ns = c->bar_timeout_ns;
+  c->A.bar_hold = c->bar_hold;
   *out = c;
   return CS_OK;
 }
@@ -1643,6 +1655,8 @@ void apply_tune(cs_ctx* c, const cs_tune_result& r) {
   c->graph_grid_per_sm = r.graph_grid_per_sm;
   c->narrow_regs = r.narrow_regs;
   c->A.narrow_regs = r.narrow_regs;
+  c->bar_sleep_ns = r.bar_sleep_ns;
+  c->A.bar_sleep_ns = r.bar_sleep_ns;
   graph_release(c);
 }
 }  // namespace
@@ -1711,6 +1725,7 @@ int cs_autotune(cs_ctx* c, int frames, cs_tune_result* out) {
     best.mx_tail_slices = c->mx_tail_slices;
     best.graph_grid_per_sm = c->graph_grid_per_sm;
     best.narrow_regs = c->narrow_regs;
+    best.bar_sleep_ns = c->bar_sleep_ns;
     time_cfg(best);  // untimed warm pass: contact buffers grow to these frames' needs
     best.frame_ms = time_cfg(best);
     // coordinate descent over the three shapes
@@ -1732,6 +1747,7 @@ int cs_autotune(cs_ctx* c, int frames, cs_tune_result* out) {
     }
     if (c->graph_mode) try_values(&cs_tune_result::graph_grid_per_sm, {4, 8, 16});
     try_values(&cs_tune_result::narrow_regs, {0, 128});
+    if (c->precision == CS_PREC_MIXED) try_values(&cs_tune_result::bar_sleep_ns, {256, 64, 0});
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     best.candidates = timed;

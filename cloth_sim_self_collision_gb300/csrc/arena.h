@@ -172,6 +172,9 @@ struct Arena {
   FrameCtl* ctl = nullptr;          // frame control on the device
   int dev_grid = 0;                 // blocks of the grid-stride narrow-phase kernels of a graph frame
   int narrow_regs = 0;              // 128: FP64 narrow-phase kernels capped at 128 registers
+  int bar_sleep_ns = 256;           // pause between polls of a waiting grid barrier
+  long long bar_timeout_ns = 2000000000;  // a waiting grid barrier gives up after this long
+  int bar_hold = 0;                 // test hook: block 0 never arrives at the grid barrier
 };
 
 // scratch for the contact pipeline (grown on demand)

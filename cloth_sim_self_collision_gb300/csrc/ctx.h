@@ -114,6 +114,11 @@ struct cs_ctx {
   int graph_grid_per_sm = 8;
   // register variant of the FP64 narrow-phase kernels (0 free, 128 capped)
   int narrow_regs = 0;
+  // pause between polls of the persistent solver's grid barrier (ns), its
+  // time-out, and the test hook that keeps block 0 from arriving
+  int bar_sleep_ns = 256;
+  long long bar_timeout_ns = 2000000000;
+  int bar_hold = 0;
   // inner FP32 solve of a refinement cycle: relative residual target and cap
   float mx_eta = 1.0e-3f;
   int mx_cap = 300;

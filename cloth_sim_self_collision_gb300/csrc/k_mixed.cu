@@ -295,7 +295,11 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
 // into one contiguous range per block, re-cut whenever a cloth stops, so blocks
 // do not idle on converged cloths (arenas of more than kRebalanceMax cloths
 // keep the static cut over all slices and skip converged cloths).
-constexpr unsigned kSpinLimit = 1u << 22;  // ~1 s of polling at the least
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 constexpr int kRebalanceMax = 2048;        // cloths whose slice prefix fits in shared memory
 
 // Grid-wide barrier on A.grid_bar with a bounded wait.  Returns false when the
@@ -308,18 +312,24 @@ __device__ bool grid_sync(const Arena& A) {
     volatile unsigned* bar = A.grid_bar;
     __threadfence();
     const unsigned gen = bar[1];
-    if (atomicAdd(&A.grid_bar[0], 1u) == gridDim.x - 1) {
+    // with the test hook set, block 0 does not arrive and every wait runs out
+    const bool hold = A.bar_hold != 0 && blockIdx.x == 0;
+    if (!hold && atomicAdd(&A.grid_bar[0], 1u) == gridDim.x - 1) {
       atomicExch(&A.grid_bar[0], 0u);
       __threadfence();
       atomicAdd(&A.grid_bar[1], 1u);
     } else {
-      unsigned n = 0;
+      // poll with a pause of A.bar_sleep_ns between reads; give up (flag the
+      // error for every block) after A.bar_timeout_ns of the device's clock
+      const unsigned long long t0 = global_ns();
+      const unsigned long long limit = (unsigned long long)A.bar_timeout_ns;
+      const unsigned ns = (unsigned)A.bar_sleep_ns;
       while (bar[1] == gen && bar[2] == 0u) {
-        if (++n > kSpinLimit) {
+        if (global_ns() - t0 > limit) {
           atomicExch(&A.grid_bar[2], 1u);
           break;
         }
-        __nanosleep(256);
+        if (ns) __nanosleep(ns);
       }
     }
     __threadfence();
