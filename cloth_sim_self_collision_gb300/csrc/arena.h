@@ -185,8 +185,10 @@ struct ContactBufs {
   // test, as (pair index, test index): face-vertex [0] and edge-edge [1]
   int q_cap[2] = {0, 0};
   int2* queue[2] = {nullptr, nullptr};
-  // continuous-collision tests the FP32 certificates left to the FP64 test
-  // (face-vertex, edge-edge; counts in counters[10], counters[11])
+  // continuous-collision tests the certificates' whole-motion stage kept for
+  // their piece stage (face-vertex, edge-edge; counts in counters[10, 11]);
+  // the tests the piece stage leaves to the FP64 test go back into queue[]
+  // (counts in counters[12, 13])
   int2* queue64[2] = {nullptr, nullptr};
   Cand* cand = nullptr;
   Cand* cand_sorted = nullptr;
@@ -198,7 +200,8 @@ struct ContactBufs {
   int* counters = nullptr;    // [0] pairs, [1] candidates, [2] contacts, [3] overflow flag,
                               // [4] zone members, [5] kept candidates, [6] / [7] face-vertex /
                               // edge-edge tests queued, [8] / [9] sorted candidates / zone
-                              // members of a graph frame
+                              // members of a graph frame, [10] / [11] CCD tests kept for the
+                              // certificates' piece stage, [12] / [13] CCD tests left to FP64
   int* level = nullptr;       // impulse level per contact
   int* order = nullptr;       // contacts grouped by level
   int* lev_cnt = nullptr;     // per cloth: level count (then offsets)

@@ -59,12 +59,6 @@ CS_HD float hi32(R32 a) {
 #endif
 }
 
-CS_HD R32 r32(double d) {
-  R32 a;
-  a.m = (float)d;
-  a.r = 1.001f * kU24 * fabsf(a.m) + 1e-37f;
-  return a;
-}
 CS_HD R32 rc(float m, float r) {
   R32 a;
   a.m = m;
@@ -98,13 +92,6 @@ CS_HD R32 operator*(float s, R32 a) {
   return c;
 }
 
-CS_HD RV rv(V3<double> d) {
-  RV a;
-  a.x = r32(d.x);
-  a.y = r32(d.y);
-  a.z = r32(d.z);
-  return a;
-}
 CS_HD RV operator+(const RV& a, const RV& b) {
   RV c;
   c.x = a.x + b.x;
@@ -317,52 +304,57 @@ CS_HD bool piece_clear(const R32 k[4], float F, bool k0_zero, float a, float h, 
   return kFV ? fv_piece_reject32(x1, x2, x3, v1, v2, v3, tm, hh) : ee_piece_reject32(x1, x2, x3, v1, v2, v3, tm, hh);
 }
 
-// The test (face-vertex when kFV, else edge-edge) rejects at whatever t
-// FindCoplanerInterp returns for x_i, v_i (i = 1, 2, 3).
-template <bool kFV>
-CS_HD bool ccd_pieces32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
-  // the cubic k0 + k1 t + k2 t^2 + k3 t^3 of FindCoplanerInterp (triple
-  // products a . (b x c)), and the magnitude of its terms: the reference's FP64
-  // rounding of the coefficients and of each evaluation stays below 4e-15 of
-  // it, and F below allows 1e-14
+// The coplanarity cubic k0 + k1 t + k2 t^2 + k3 t^3 of FindCoplanerInterp
+// (triple products a . (b x c) of x_i and v_i), with F, a bound on the
+// reference's FP64 rounding of its coefficients and of each evaluation: below
+// 4e-15 of the magnitude of the terms, F allows 1e-14.  k0_zero: the FP64 k0
+// may be exactly 0, which sends the bisection to t = 1 - 2^-15.
+struct Cubic32 {
   R32 k[4];
+  float F;
+  bool k0_zero;
+};
+CS_HD Cubic32 coplanar_cubic32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2,
+                               const RV& v3) {
+  Cubic32 c;
   float mk = 0.f;
-  {
-    const RV* X[3] = {&x1, &x2, &x3};
-    const RV* V[3] = {&v1, &v2, &v3};
-    // stp(c3, c1, c2) with each c_i = x_i (bit clear) or v_i (bit set); the
-    // bits set count the power of t
-    R32 acc[4] = {rc(0.f, 0.f), rc(0.f, 0.f), rc(0.f, 0.f), rc(0.f, 0.f)};
-    for (int s = 0; s < 8; s++) {
-      const RV& c1 = (s & 1) ? *V[0] : *X[0];
-      const RV& c2 = (s & 2) ? *V[1] : *X[1];
-      const RV& c3 = (s & 4) ? *V[2] : *X[2];
-      const R32 t = rdot(c3, rcross(c1, c2));
-      const int deg = (s & 1) + ((s >> 1) & 1) + ((s >> 2) & 1);
-      acc[deg] = acc[deg] + t;
-      mk += fabsf(t.m) + t.r +
-            (fabsf(c3.x.m) + c3.x.r) * ((fabsf(c1.y.m) + c1.y.r) * (fabsf(c2.z.m) + c2.z.r) +
-                                        (fabsf(c1.z.m) + c1.z.r) * (fabsf(c2.y.m) + c2.y.r)) +
-            (fabsf(c3.y.m) + c3.y.r) * ((fabsf(c1.z.m) + c1.z.r) * (fabsf(c2.x.m) + c2.x.r) +
-                                        (fabsf(c1.x.m) + c1.x.r) * (fabsf(c2.z.m) + c2.z.r)) +
-            (fabsf(c3.z.m) + c3.z.r) * ((fabsf(c1.x.m) + c1.x.r) * (fabsf(c2.y.m) + c2.y.r) +
-                                        (fabsf(c1.y.m) + c1.y.r) * (fabsf(c2.x.m) + c2.x.r));
-    }
-    for (int d = 0; d < 4; d++) k[d] = acc[d];
+  const RV* X[3] = {&x1, &x2, &x3};
+  const RV* V[3] = {&v1, &v2, &v3};
+  // stp(c3, c1, c2) with each c_i = x_i (bit clear) or v_i (bit set); the
+  // bits set count the power of t
+  R32 acc[4] = {rc(0.f, 0.f), rc(0.f, 0.f), rc(0.f, 0.f), rc(0.f, 0.f)};
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    const RV& c1 = (s & 1) ? *V[0] : *X[0];
+    const RV& c2 = (s & 2) ? *V[1] : *X[1];
+    const RV& c3 = (s & 4) ? *V[2] : *X[2];
+    const R32 t = rdot(c3, rcross(c1, c2));
+    const int deg = (s & 1) + ((s >> 1) & 1) + ((s >> 2) & 1);
+    acc[deg] = acc[deg] + t;
+    mk += fabsf(t.m) + t.r +
+          (fabsf(c3.x.m) + c3.x.r) * ((fabsf(c1.y.m) + c1.y.r) * (fabsf(c2.z.m) + c2.z.r) +
+                                      (fabsf(c1.z.m) + c1.z.r) * (fabsf(c2.y.m) + c2.y.r)) +
+          (fabsf(c3.y.m) + c3.y.r) * ((fabsf(c1.z.m) + c1.z.r) * (fabsf(c2.x.m) + c2.x.r) +
+                                      (fabsf(c1.x.m) + c1.x.r) * (fabsf(c2.z.m) + c2.z.r)) +
+          (fabsf(c3.z.m) + c3.z.r) * ((fabsf(c1.x.m) + c1.x.r) * (fabsf(c2.y.m) + c2.y.r) +
+                                      (fabsf(c1.y.m) + c1.y.r) * (fabsf(c2.x.m) + c2.x.r));
   }
-  const float F = 1.0e-14f * mk + 1e-30f;
-  // a coefficient that may be exactly 0 in FP64 at t = 0 sends the bisection to
-  // t = 1 - 2^-15: the piece that ends at 1 is then tested as well
-  const bool k0_zero = !(lo32(k[0]) > F || hi32(k[0]) < -F);
-  // no sign change on all of [0, 1]: FindCoplanerInterp returns -1
-  if (!k0_zero && cubic_one_sign(k, F, 0.f, 1.f)) return true;
-  // edge-edge: the edges' hulls over the whole motion more than 1e-2 apart
-  if (!kFV && ee_hull_far32(x1, x2, x3, v1, v2, v3, 0.5f, 0.5f)) return true;
-  // pieces of 1/8, halved down to 1/32 where a piece that may hold t fails:
-  // each eighth is a tree of 7 nodes in preorder (0: the eighth; 1, 4: its
-  // halves; 2, 3 and 5, 6: their halves), a node tested only if its parent
-  // failed, and a failing leaf ends the certificate (one call site, so the
-  // piece certificate is compiled once)
+#pragma unroll
+  for (int d = 0; d < 4; d++) c.k[d] = acc[d];
+  c.F = 1.0e-14f * mk + 1e-30f;
+  c.k0_zero = !(lo32(c.k[0]) > c.F || hi32(c.k[0]) < -c.F);
+  return c;
+}
+
+// The test (face-vertex when kFV, else edge-edge) rejects at whatever t
+// FindCoplanerInterp returns, piece by piece: pieces of 1/8, halved down to
+// 1/32 where a piece that may hold t fails.  Each eighth is a tree of 7 nodes
+// in preorder (0: the eighth; 1, 4: its halves; 2, 3 and 5, 6: their halves),
+// a node tested only if its parent failed, and a failing leaf ends the
+// certificate (one call site, so the piece certificate is compiled once).
+template <bool kFV>
+CS_HD bool ccd_pieces32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3,
+                        const Cubic32& c) {
 #pragma unroll 1
   for (int j = 0; j < 8; j++) {
     unsigned need = 1u;
@@ -371,7 +363,7 @@ CS_HD bool ccd_pieces32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, 
       if (!((need >> n) & 1u)) continue;
       const float off = n == 3 ? 0.03125f : (n == 4 || n == 5) ? 0.0625f : n == 6 ? 0.09375f : 0.f;
       const float h = n == 0 ? 0.125f : (n == 1 || n == 4) ? 0.0625f : 0.03125f;
-      if (piece_clear<kFV>(k, F, k0_zero, 0.125f * (float)j + off, h, x1, x2, x3, v1, v2, v3)) continue;
+      if (piece_clear<kFV>(c.k, c.F, c.k0_zero, 0.125f * (float)j + off, h, x1, x2, x3, v1, v2, v3)) continue;
       if (n == 0)
         need |= (1u << 1) | (1u << 4);
       else if (n == 1)
@@ -385,22 +377,28 @@ CS_HD bool ccd_pieces32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, 
   return true;
 }
 
+// x_i, v_i of the face-vertex test (face p0 p1 p2, vertex p3) and of the
+// edge-edge test (edges p0 p1 and q0 q1) from the points' hi/lo parts
+CS_HD void ccd_xv(const PS& s0, const PS& s1, const PS& s2, const PS& s3, RV& x1, RV& x2, RV& x3, RV& v1, RV& v2,
+                  RV& v3) {
+  hl_xv(s0, s1, x1, v1);
+  hl_xv(s0, s2, x2, v2);
+  hl_xv(s0, s3, x3, v3);
+}
 
-// True when IsContact_FV_CCD certainly rejects the face p0 p1 p2 and the vertex
-// p3 moving to q0..q3, from enclosures of the differences FindCoplanerInterp
-// forms (x_i = p_i - p0, v_i = (q_i - q0) - x_i): the vertex stays on one side
-// of the start face plane (the test's sign block, bvh_aabb.cpp:683-690: the
-// four heights (p0 - p3).n, (q0 - q3).n, (q1 - q3).n, (q2 - q3).n with
-// n = x1 x2, each beyond twice its bound, which also covers the reference's FP64
-// rounding, and 1e-30, so that its products keep their signs), the four points
-// are never coplanar in [0, 1], or at any coplanarity time the vertex projects
-// outside the face.
-CS_HD bool fv_ccd_cert32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
+// IsContact_FV_CCD certainly rejects over the whole motion: the vertex stays
+// on one side of the start face plane (the test's sign block,
+// bvh_aabb.cpp:683-690: the four heights (p0 - p3).n, (q0 - q3).n,
+// (q1 - q3).n, (q2 - q3).n with n = x1 x2, each beyond twice its bound, which
+// also covers the reference's FP64 rounding, and 1e-30, so that its products
+// keep their signs), or the four points are never coplanar in [0, 1].
+CS_HD bool fv_ccd_whole32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
   {
     const RV n = rcross(x1, x2);
     const RV e3 = x3 + v3;  // q3 - q0
     const R32 h[4] = {-rdot(x3, n), -rdot(e3, n), rdot((x1 + v1) - e3, n), rdot((x2 + v2) - e3, n)};
     bool pos = true, neg = true;
+#pragma unroll
     for (int i = 0; i < 4; i++) {
       const R32 w = rc(h[i].m, 2.f * h[i].r);
       pos = pos && lo32(w) > 1e-30f;
@@ -408,32 +406,39 @@ CS_HD bool fv_ccd_cert32(const RV& x1, const RV& x2, const RV& x3, const RV& v1,
     }
     if (pos || neg) return true;
   }
-  return ccd_pieces32<true>(x1, x2, x3, v1, v2, v3);
-}
-// the same from the points' hi/lo parts (face p0 p1 p2, vertex p3)
-CS_HD bool fv_ccd_cert32(const PS& s0, const PS& s1, const PS& s2, const PS& s3) {
-  RV x1, x2, x3, v1, v2, v3;
-  hl_xv(s0, s1, x1, v1);
-  hl_xv(s0, s2, x2, v2);
-  hl_xv(s0, s3, x3, v3);
-  return fv_ccd_cert32(x1, x2, x3, v1, v2, v3);
+  const Cubic32 c = coplanar_cubic32(x1, x2, x3, v1, v2, v3);
+  return !c.k0_zero && cubic_one_sign(c.k, c.F, 0.f, 1.f);
 }
 
-// True when IsContact_EE_CCD certainly rejects the edges p0 p1 and q0 q1 moving
-// to their end points, from enclosures of x1 = p1 - p0, x2 = q0 - p0,
-// x3 = q1 - p0 and their changes v_i (as FindCoplanerInterp forms them): no coplanarity in
-// [0, 1], the edges more than 1e-2 apart over the whole motion, or at any
-// coplanarity time a ratio out of range or the edges apart.
-CS_HD bool ee_ccd_cert32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
-  return ccd_pieces32<false>(x1, x2, x3, v1, v2, v3);
+// IsContact_EE_CCD certainly rejects over the whole motion: no coplanarity in
+// [0, 1], or the edges more than 1e-2 apart throughout.
+CS_HD bool ee_ccd_whole32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
+  const Cubic32 c = coplanar_cubic32(x1, x2, x3, v1, v2, v3);
+  if (!c.k0_zero && cubic_one_sign(c.k, c.F, 0.f, 1.f)) return true;
+  return ee_hull_far32(x1, x2, x3, v1, v2, v3, 0.5f, 0.5f);
 }
-// the same from the points' hi/lo parts (edges p0 p1 and q0 q1)
+
+// The piece stage on its own (after the whole-motion stage kept the test):
+// at any coplanarity time the vertex projects outside the face (face-vertex),
+// or a ratio is out of range or the edges are apart (edge-edge).
+template <bool kFV>
+CS_HD bool ccd_pieces_stage32(const RV& x1, const RV& x2, const RV& x3, const RV& v1, const RV& v2, const RV& v3) {
+  return ccd_pieces32<kFV>(x1, x2, x3, v1, v2, v3, coplanar_cubic32(x1, x2, x3, v1, v2, v3));
+}
+
+// Both stages: true when IsContact_FV_CCD (the face p0 p1 p2 and the vertex p3
+// moving to their end points) or IsContact_EE_CCD (the edges p0 p1 and q0 q1)
+// certainly rejects, from enclosures of the differences FindCoplanerInterp
+// forms (x_i = p_i - p0, v_i = (q_i - q0) - x_i).
+CS_HD bool fv_ccd_cert32(const PS& s0, const PS& s1, const PS& s2, const PS& s3) {
+  RV x1, x2, x3, v1, v2, v3;
+  ccd_xv(s0, s1, s2, s3, x1, x2, x3, v1, v2, v3);
+  return fv_ccd_whole32(x1, x2, x3, v1, v2, v3) || ccd_pieces_stage32<true>(x1, x2, x3, v1, v2, v3);
+}
 CS_HD bool ee_ccd_cert32(const PS& p0, const PS& p1, const PS& q0, const PS& q1) {
   RV x1, x2, x3, v1, v2, v3;
-  hl_xv(p0, p1, x1, v1);
-  hl_xv(p0, q0, x2, v2);
-  hl_xv(p0, q1, x3, v3);
-  return ee_ccd_cert32(x1, x2, x3, v1, v2, v3);
+  ccd_xv(p0, p1, q0, q1, x1, x2, x3, v1, v2, v3);
+  return ee_ccd_whole32(x1, x2, x3, v1, v2, v3) || ccd_pieces_stage32<false>(x1, x2, x3, v1, v2, v3);
 }
 
 }  // namespace cs

@@ -522,19 +522,51 @@ __device__ __forceinline__ void narrow_fv_body(const Arena& A, const ContactBufs
       // four points are never coplanar in [0, 1] (FindCoplanerInterp returns
       // -1), or at any coplanarity time the vertex projects outside the face;
       // from enclosures of the FP64 differences the FP64 test itself forms
-      if (fv_ccd_cert32(ld_ps(A, f0), ld_ps(A, f1), ld_ps(A, f2), ld_ps(A, q))) continue;
-      // left to the FP64 test (k_narrow_fv64), in a packed queue
+      // (the whole-motion stage here, the piece stage on the packed survivors
+      // in k_narrow_fv_pieces, so each stage's warps stay full)
+      RV x1, x2, x3, v1, v2, v3;
+      ccd_xv(ld_ps(A, f0), ld_ps(A, f1), ld_ps(A, f2), ld_ps(A, q), x1, x2, x3, v1, v2, v3);
+      if (fv_ccd_whole32(x1, x2, x3, v1, v2, v3)) continue;
       C.queue64[0][warp_append(&C.counters[10])] = it;
     }
+  }
+}
+
+// The piece stage of the certificates on the tests the whole-motion stage
+// kept (queue64[kind], counters[10 + kind]); the tests it cannot reject go to
+// the FP64 test, packed into queue[kind] (free again after pass 2),
+// counters[12 + kind].
+template <bool kFV>
+__device__ __forceinline__ void narrow_pieces_body(const Arena& A, const ContactBufs& C) {
+  constexpr int kind = kFV ? 0 : 1;
+  const int n = __ldcg(&C.counters[10 + kind]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 it = C.queue64[kind][i];
+    const int2 pr = C.pairs[it.x];
+    const int ta = A.node[3 * pr.x + 1], tb = A.node[3 * pr.y + 1];
+    int a, b, c, d;
+    if (kFV) {
+      const bool fa = it.y < 3;
+      const int tf = fa ? ta : tb, tv = fa ? tb : ta, k = fa ? it.y : it.y - 3;
+      a = A.tri[3 * tf], b = A.tri[3 * tf + 1], c = A.tri[3 * tf + 2], d = A.tri[3 * tv + k];
+    } else {
+      const int k = it.y - 6;
+      a = A.tri[3 * ta + kEE[k][0]], b = A.tri[3 * ta + kEE[k][1]];
+      c = A.tri[3 * tb + kEE[k][2]], d = A.tri[3 * tb + kEE[k][3]];
+    }
+    RV x1, x2, x3, v1, v2, v3;
+    ccd_xv(ld_ps(A, a), ld_ps(A, b), ld_ps(A, c), ld_ps(A, d), x1, x2, x3, v1, v2, v3);
+    if (ccd_pieces_stage32<kFV>(x1, x2, x3, v1, v2, v3)) continue;
+    C.queue[kind][warp_append(&C.counters[12 + kind])] = it;
   }
 }
 
 // the face-vertex continuous-collision tests the certificates left (FP64)
 __device__ __forceinline__ void narrow_fv64_body(const Arena& A, const ContactBufs& C, const double* xs,
                                                  const double* vs) {
-  const int n = __ldcg(&C.counters[10]);
+  const int n = __ldcg(&C.counters[12]);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int2 it = C.queue64[0][i];
+    const int2 it = C.queue[0][i];
     const int2 pr = C.pairs[it.x];
     const int na = pr.x, nb = pr.y, test = it.y;
     const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
@@ -589,7 +621,11 @@ __device__ __forceinline__ void narrow_ee_body(const Arena& A, const ContactBufs
       // in [0, 1], the edges more than the test's 1e-2 apart over the whole
       // motion, or at any coplanarity time a ratio out of range or the edges
       // apart; from enclosures of the vectors coplanar_time forms
-      if (ee_ccd_cert32(ld_ps(A, i0), ld_ps(A, i1), ld_ps(A, j0), ld_ps(A, j1))) continue;
+      // (the whole-motion stage here, the piece stage on the packed survivors
+      // in k_narrow_ee_pieces)
+      RV x1, x2, x3, v1, v2, v3;
+      ccd_xv(ld_ps(A, i0), ld_ps(A, i1), ld_ps(A, j0), ld_ps(A, j1), x1, x2, x3, v1, v2, v3);
+      if (ee_ccd_whole32(x1, x2, x3, v1, v2, v3)) continue;
       C.queue64[1][warp_append(&C.counters[11])] = it;
     }
   }
@@ -598,9 +634,9 @@ __device__ __forceinline__ void narrow_ee_body(const Arena& A, const ContactBufs
 // the edge-edge continuous-collision tests the certificates left (FP64)
 __device__ __forceinline__ void narrow_ee64_body(const Arena& A, const ContactBufs& C, const double* xs,
                                                  const double* vs) {
-  const int n = __ldcg(&C.counters[11]);
+  const int n = __ldcg(&C.counters[13]);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int2 it = C.queue64[1][i];
+    const int2 it = C.queue[1][i];
     const int2 pr = C.pairs[it.x];
     const int na = pr.x, nb = pr.y, test = it.y;
     const int ta = A.node[3 * na + 1], tb = A.node[3 * nb + 1];
@@ -624,6 +660,8 @@ __global__ void __launch_bounds__(kT, 4) k_narrow_ee_b4(Arena A, ContactBufs C, 
                                                         const double* vs, double delta_override) {
   narrow_ee_body(A, C, ccd, xs, vs, delta_override);
 }
+__global__ void k_narrow_fv_pieces(Arena A, ContactBufs C) { narrow_pieces_body<true>(A, C); }
+__global__ void k_narrow_ee_pieces(Arena A, ContactBufs C) { narrow_pieces_body<false>(A, C); }
 __global__ void k_narrow_fv64(Arena A, ContactBufs C, const double* xs, const double* vs) {
   narrow_fv64_body(A, C, xs, vs);
 }
@@ -662,6 +700,13 @@ void narrow_fp64_passes(const Arena& A, const ContactBufs& C, int ccd, const dou
     k_narrow_ee<<<grid, kT, 0, s>>>(A, C, ccd, xs, vs, delta_override);
   prof_end(PK_NARROW_EE, s);
   if (!ccd) return;
+  prof_begin(PK_NARROW_FV, s);
+  k_narrow_fv_pieces<<<grid, kT, 0, s>>>(A, C);
+  prof_end(PK_NARROW_FV, s);
+  prof_begin(PK_NARROW_EE, s);
+  k_narrow_ee_pieces<<<grid, kT, 0, s>>>(A, C);
+  prof_end(PK_NARROW_EE, s);
+  g_launches += 2;
   prof_begin(PK_NARROW_CCD64, s);
   if (b4) {
     k_narrow_fv64_b4<<<grid, kT, 0, s>>>(A, C, xs, vs);
@@ -1177,7 +1222,7 @@ void launch_narrow(const Arena& A, const ContactBufs& C, int ccd, const double* 
     grid2 = 8 * (sms > 0 ? sms : 1);
   }
   prof_begin(PK_NARROW, s);
-  cudaMemsetAsync(C.counters + 6, 0, 6 * sizeof(int), s);  // queue counts [6, 7], [10, 11]
+  cudaMemsetAsync(C.counters + 6, 0, 8 * sizeof(int), s);  // queue counts [6, 7], [10, 13]
   prof_begin(PK_NARROW_FILTER, s);
   k_narrow_filter<<<nblk(npairs), kT, 0, s>>>(A, C, ccd, delta_override, npairs);
   prof_end(PK_NARROW_FILTER, s);
@@ -1526,7 +1571,7 @@ __global__ void k_riz_velocity_dev(ContactBufs C, int S, const double* xs, doubl
 
 void launch_narrow_dev(const Arena& A, const ContactBufs& C, int ccd, const double* xs, const double* vs,
                        cudaStream_t s) {
-  launch_check(cudaMemsetAsync(C.counters + 6, 0, 6 * sizeof(int), s), "cudaMemsetAsync");
+  launch_check(cudaMemsetAsync(C.counters + 6, 0, 8 * sizeof(int), s), "cudaMemsetAsync");
   k_narrow_filter_dev<<<dev_grid(A), kT, 0, s>>>(A, C, ccd, -1.0);
   narrow_fp64_passes(A, C, ccd, xs, vs, -1.0, dev_grid(A), s);
   g_launches += 3;
