@@ -412,6 +412,7 @@ void install(cs_ctx* c, ArenaSet& o) {
   graph_release(c);
   o.A.narrow_regs = c->narrow_regs;
   o.A.bar_sleep_ns = c->bar_sleep_ns;
+  o.A.mx_eta_big = c->mx_eta_big;
   o.A.bar_timeout_ns = c->bar_timeout_ns;
   o.A.bar_hold = c->bar_hold;
   std::swap(c->A, o.A);
@@ -994,6 +995,7 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_MX_PERSISTENT")) c->mx_persistent = std::atoi(e) != 0;
   if (const char* e = std::getenv("CLOTHGPU_MX_BLOCKS_PER_SM")) c->mx_blocks_per_sm = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_ETA")) c->mx_eta = (float)std::atof(e);
+  if (const char* e = std::getenv("CLOTHGPU_MX_ETA_BIG")) c->mx_eta_big = (float)std::atof(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_THREADS")) c->mx_threads = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_CAP")) c->mx_cap = std::atoi(e);
   if (const char* e = std::getenv("CLOTHGPU_MX_TAIL_SLICES")) c->mx_tail_slices = std::atoi(e);
@@ -1008,6 +1010,7 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_BAR_HOLD")) c->bar_hold = std::atoi(e) != 0;
   c->A.narrow_regs = c->narrow_regs;
   c->A.bar_sleep_ns = c->bar_sleep_ns;
+  c->A.mx_eta_big = c->mx_eta_big;
   c->A.bar_timeout_ns = c->bar_timeout_ns;
   c->A.bar_hold = c->bar_hold;
   *out = c;

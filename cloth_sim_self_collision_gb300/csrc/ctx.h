@@ -121,6 +121,7 @@ struct cs_ctx {
   int bar_hold = 0;
   // inner FP32 solve of a refinement cycle: relative residual target and cap
   float mx_eta = 1.0e-3f;
+  float mx_eta_big = 1.0e-4f;  // inner tolerance of cloths over 16384 vertices
   int mx_cap = 300;
   // per slot: the cloth blew up (CS_ERR_DIVERGED) and is no longer stepped
   std::vector<int> dead;
