@@ -56,10 +56,6 @@ struct InstState {
   // barrier that follows); alpha and beta as the cloth's last block left them
   double gam, alf;
   int istop;
-  // the persistent inner solve continues the previous cycle's Krylov
-  // directions (p, s) after the FP64 residual replaced its own, instead of
-  // restarting (set when a cycle ends without a breakdown)
-  int cont;
   int bjac;          // the inner solve runs on the block-Jacobi-scaled matrix
   float alpha32, beta32;
   // frame control on the device (a frame captured in a CUDA graph): the cloth

@@ -146,17 +146,12 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_inner_init(Arena A) {
 #pragma unroll
       for (int k = 0; k < 3; k++) r[k] = (float)A.r[3 * c.row + k];
     }
-    // a cloth that continues its directions keeps p and brings s to the buffer
-    // iteration 1 reads (s32b): its last iteration wrote s to s32 when odd
-    const InstState& St = A.st[c.inst];
-    const bool cont = St.cont != 0;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       A.r32[3 * c.row + k] = r[k];
       A.d32[3 * c.row + k] = 0.f;
       A.z32[3 * c.row + k] = r[k];
-      if (!cont) A.p32[3 * c.row + k] = r[k];
-      if (cont && (St.inner_iters & 1)) A.s32b[3 * c.row + k] = A.s32[3 * c.row + k];
+      A.p32[3 * c.row + k] = r[k];
       rr += r[k] * r[k];
     }
   }
@@ -516,13 +511,11 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads)
     float* Rn = odd ? A.r32b : A.r32;
     float* Wn = odd ? A.w32b : A.w32;
     float* Sn = odd ? A.s32 : A.s32b;
+    const bool first = it == 1;
     for (int inst = R.c0; inst <= R.c1; inst++) {
       int lo, hi;
       if (!portion(A, R, compact, s_pref, inst, lo, hi)) continue;
       const InstState& St = A.st[inst];
-      // iteration 1 of a restart reads no s, p; a continuing cloth reads the
-      // last cycle's
-      const bool first = it == 1 && !St.cont;
       const float alpha = St.alpha32;
       const float beta = first ? 0.f : St.beta32;
       for (int sl = lo + warp; sl < hi; sl += kPersistWarps) {
@@ -585,7 +578,6 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads)
           if (gam <= e * e * Sw.rr_in0 || it >= cap || !(den > 0.0)) {
             Sw.istop = 1;
             Sw.idone = 1;
-            Sw.cont = den > 0.0 ? 1 : 0;
             Sw.red[2] = gam;
             atomicSub(&A.grid_bar[3], 1u);
           } else {
@@ -649,23 +641,10 @@ __global__ void k_mx_pstart(Arena A) {
   if ((threadIdx.x & 31) == 0) {
     InstState& S = A.st[inst];
     S.rr_in0 = gam;
-    // continuing: the replaced residual r enters the recurrence as r_{k+1}
-    // (beta = r.r / the last cycle's r_k.r_k, alpha from the single-reduction
-    // formula with the last cycle's alpha); a breakdown restarts
-    double beta = 0.0, alf = del > 0.0 ? gam / del : 0.0;
-    if (S.cont) {
-      const double b = gam / S.gam, den = del - b * gam / S.alf;
-      if (S.gam > 0.0 && S.alf > 0.0 && den > 0.0) {
-        beta = b;
-        alf = gam / den;
-      } else {
-        S.cont = 0;
-      }
-    }
     S.gam = gam;
-    S.alf = alf;
+    S.alf = del > 0.0 ? gam / del : 0.0;
     S.alpha32 = (float)S.alf;
-    S.beta32 = (float)beta;
+    S.beta32 = 0.f;
     S.idone = (gam <= 0.0 || !(del > 0.0)) ? 1 : 0;
     S.istop = S.idone;
     S.inner_iters = 0;
@@ -722,7 +701,6 @@ __global__ void k_mx_outer_start(Arena A) {
   S.cycles = 0;
   S.total_iters = 0;
   S.idone = 0;
-  S.cont = 0;
   {
     const float lo = __uint_as_float(A.dg_range[2 * inst]), hi = __uint_as_float(A.dg_range[2 * inst + 1]);
     S.bjac = hi > kJacobiSpread * lo;
