@@ -1,5 +1,6 @@
 // prof.cu -- per-kernel CUDA-event timing (see prof.h).
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "prof.h"
@@ -19,6 +20,8 @@ struct Pending {
   cudaEvent_t a, b;
 };
 bool g_on = false;
+// the serving loop's worker and builder threads may both launch profiled kernels
+std::mutex g_mu;
 std::vector<Pending> g_pending;
 std::vector<cudaEvent_t> g_free;
 cudaEvent_t g_open[PK_COUNT];
@@ -44,23 +47,28 @@ cudaEvent_t get_event() {
 
 bool prof_enabled() { return g_on; }
 
+// prof_collect with the lock held
+void collect_locked();
+
 void prof_enable(bool on) { g_on = on; }
 
 void prof_begin(ProfKernel k, cudaStream_t s) {
   if (!g_on) return;
+  std::lock_guard<std::mutex> lock(g_mu);
   g_open[k] = get_event();
   cudaEventRecord(g_open[k], s);
 }
 
 void prof_end(ProfKernel k, cudaStream_t s) {
   if (!g_on) return;
+  std::lock_guard<std::mutex> lock(g_mu);
   cudaEvent_t b = get_event();
   cudaEventRecord(b, s);
   g_pending.push_back({(int)k, g_open[k], b});
-  if (g_pending.size() > 4096) prof_collect();
+  if (g_pending.size() > 4096) collect_locked();
 }
 
-void prof_collect() {
+void collect_locked() {
   for (Pending& p : g_pending) {
     float ms = 0;
     cudaEventSynchronize(p.b);
@@ -72,6 +80,11 @@ void prof_collect() {
     g_free.push_back(p.b);
   }
   g_pending.clear();
+}
+
+void prof_collect() {
+  std::lock_guard<std::mutex> lock(g_mu);
+  collect_locked();
 }
 
 void prof_reset() {
