@@ -356,16 +356,16 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
     A.val32 = m.alloc<float>(vtot);
     CK(cudaMemsetAsync(A.val32, 0, sizeof(float) * (size_t)std::max(vtot, 1LL), s));
     A.linv32 = m.alloc<float>(9 * (size_t)NV);
-    A.r32 = m.alloc<float>(3 * (size_t)NV);
-    A.r32b = m.alloc<float>(3 * (size_t)NV);
-    A.w32 = m.alloc<float>(3 * (size_t)NV);
-    A.w32b = m.alloc<float>(3 * (size_t)NV);
-    A.s32 = m.alloc<float>(3 * (size_t)NV);
-    A.s32b = m.alloc<float>(3 * (size_t)NV);
-    A.d32 = m.alloc<float>(3 * (size_t)NV);
-    A.p32 = m.alloc<float>(3 * (size_t)NV);
-    A.q32 = m.alloc<float>(3 * (size_t)NV);
-    A.z32 = m.alloc<float>(3 * (size_t)NV);
+    A.r32 = m.alloc<float>(4 * (size_t)NV);
+    A.r32b = m.alloc<float>(4 * (size_t)NV);
+    A.w32 = m.alloc<float>(4 * (size_t)NV);
+    A.w32b = m.alloc<float>(4 * (size_t)NV);
+    A.s32 = m.alloc<float>(4 * (size_t)NV);
+    A.s32b = m.alloc<float>(4 * (size_t)NV);
+    A.d32 = m.alloc<float>(4 * (size_t)NV);
+    A.p32 = m.alloc<float>(4 * (size_t)NV);
+    A.q32 = m.alloc<float>(4 * (size_t)NV);
+    A.z32 = m.alloc<float>(4 * (size_t)NV);
     A.part32 = m.alloc<double>(3 * (size_t)std::max(A.nslice, 1));
     {
       std::vector<long long> sb(A.nslice, 0);
@@ -950,7 +950,7 @@ size_t cloth_device_bytes(const ClothTopo& t) {
   b += np * (24 + 3 * 4) + t.edge_uv.size() * 4;  // vertex boxes (FP32), dirty / zone flags, edges
   const size_t sell = ((np + 31) / 32) * 32 * 16;  // SELL entries, padded to the slice width
   b += sell * (36 + 4) + (nb + np) * 8;        // FP32 values, columns, SELL positions
-  b += np * (36 + 5 * 12);                     // FP32 diagonal inverse and vectors
+  b += np * (36 + 10 * 16);                    // FP32 diagonal inverse and the 10 solver vectors (16 B each)
   // pairs, the test queues and their FP64 queues (2.5 pair capacities each),
   // and the candidate buffers
   b += (16 * nt + 4096) * 8 * 6 + (4 * nt + 4096) * 120;

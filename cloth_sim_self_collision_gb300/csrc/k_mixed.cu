@@ -130,6 +130,16 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_scale(Arena A) {
 
 // r32 = S r (scaled cloths) or r, from the FP64 residual; d = 0, z = p = r32;
 // slice partials of r.r (fields 1 and 2: r.z equals r.r without a preconditioner)
+// The FP32 vectors of the inner solve (r, w, s, p, d, z, q) keep a vertex's
+// x, y, z and a pad in 16 bytes: one aligned load or store per vertex.
+constexpr int kV = 4;
+__device__ __forceinline__ float4 ld_v4(const float* a, int v) {
+  return *reinterpret_cast<const float4*>(a + kV * (size_t)v);
+}
+__device__ __forceinline__ void st_v4(float* a, int v, const float x[3]) {
+  *reinterpret_cast<float4*>(a + kV * (size_t)v) = make_float4(x[0], x[1], x[2], 0.f);
+}
+
 __global__ void __launch_bounds__(kSliceThreads) k_mx_inner_init(Arena A) {
   SliceCtx c;
   if (!slice_ctx(A, c, false)) return;
@@ -148,10 +158,10 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_inner_init(Arena A) {
     }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      A.r32[3 * c.row + k] = r[k];
-      A.d32[3 * c.row + k] = 0.f;
-      A.z32[3 * c.row + k] = r[k];
-      A.p32[3 * c.row + k] = r[k];
+      A.r32[kV * c.row + k] = r[k];
+      A.d32[kV * c.row + k] = 0.f;
+      A.z32[kV * c.row + k] = r[k];
+      A.p32[kV * c.row + k] = r[k];
       rr += r[k] * r[k];
     }
   }
@@ -185,7 +195,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_spmv(Arena A) {
   float y0 = 0.f, y1 = 0.f, y2 = 0.f;
   for (int j = 0; j < w; j++) {
     const int col = Cc[32 * j];
-    const float x0 = A.p32[3 * col + 0], x1 = A.p32[3 * col + 1], x2 = A.p32[3 * col + 2];
+    const float x0 = A.p32[kV * col + 0], x1 = A.p32[kV * col + 1], x2 = A.p32[kV * col + 2];
     const float* v = V + 288 * j;
     y0 = fmaf(v[0], x0, fmaf(v[32], x1, fmaf(v[64], x2, y0)));
     y1 = fmaf(v[96], x0, fmaf(v[128], x1, fmaf(v[160], x2, y1)));
@@ -193,10 +203,10 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_spmv(Arena A) {
   }
   float pq = 0.f;
   if (c.valid) {
-    A.q32[3 * c.row + 0] = y0;
-    A.q32[3 * c.row + 1] = y1;
-    A.q32[3 * c.row + 2] = y2;
-    pq = A.p32[3 * c.row + 0] * y0 + A.p32[3 * c.row + 1] * y1 + A.p32[3 * c.row + 2] * y2;
+    A.q32[kV * c.row + 0] = y0;
+    A.q32[kV * c.row + 1] = y1;
+    A.q32[kV * c.row + 2] = y2;
+    pq = A.p32[kV * c.row + 0] * y0 + A.p32[kV * c.row + 1] * y1 + A.p32[kV * c.row + 2] * y2;
   }
   pq = warp_sum_f(pq);
   if (c.lane == 0) {
@@ -217,7 +227,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_update(Arena A, int it) {
     float r[3], z[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      const int i = 3 * c.row + k;
+      const int i = kV * c.row + k;
       A.d32[i] = fmaf(alpha, A.p32[i], A.d32[i]);
       r[k] = fmaf(-alpha, A.q32[i], A.r32[i]);
       A.r32[i] = r[k];
@@ -225,7 +235,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_update(Arena A, int it) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       z[k] = r[k];
-      A.z32[3 * c.row + k] = z[k];
+      A.z32[kV * c.row + k] = z[k];
       rz += r[k] * z[k];
       rr += r[k] * r[k];
     }
@@ -239,7 +249,6 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_update(Arena A, int it) {
   finish_cloth(A, c.inst, c.lane, 1, 2);
 }
 
-// inner convergence (|r|^2 <= eta^2 |r0|^2 or the cap), beta, p = z + beta p
 // The inner tolerance of cloth inst: eta, or eta_big for cloths of more than
 // kBigClothRows rows.  A large stiff sheet needs many inner iterations per
 // refinement cycle, and each cycle restarts its Krylov space: measured on the
@@ -251,6 +260,7 @@ __device__ __forceinline__ float inner_eta(const Arena& A, int inst, float eta) 
   return A.voff[inst + 1] - A.voff[inst] > kBigClothRows ? fminf(eta, A.mx_eta_big) : eta;
 }
 
+// inner convergence (|r|^2 <= eta^2 |r0|^2 or the cap), beta, p = z + beta p
 __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it, float eta, int cap) {
   SliceCtx c;
   if (!slice_ctx(A, c, true)) return;
@@ -269,7 +279,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_direction(Arena A, int it,
   if (c.valid) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      const int i = 3 * c.row + k;
+      const int i = kV * c.row + k;
       A.p32[i] = fmaf(beta, A.p32[i], A.z32[i]);
     }
   }
@@ -466,8 +476,11 @@ __device__ __forceinline__ bool portion(const Arena& A, const PersistRange& R, b
   return lo < hi;
 }
 
-template <int kPersistThreads>
-__global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads)
+// kMinBlocks: the blocks per SM the build keeps room for (256 threads and 6
+// blocks: 40 registers a thread, a few spills; 4 blocks: 64 registers, none);
+// the launch picks the build for the blocks per SM it runs
+template <int kPersistThreads, int kMinBlocks = 1536 / kPersistThreads>
+__global__ void __launch_bounds__(kPersistThreads, kMinBlocks)
     k_mx_persist(Arena A, float eta, int cap, int exit_slices, int resume) {
   constexpr int kPersistWarps = kPersistThreads / 32;
   __shared__ double sh[kPersistWarps];
@@ -527,13 +540,12 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads)
 #pragma unroll 2
         for (int j = 0; j < w; j++) {
           const int col = Cc[32 * j];
-          float x[3];
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            const int i = 3 * col + k;
-            const float sk = first ? Wc[i] : fmaf(beta, Sp[i], Wc[i]);
-            x[k] = fmaf(-alpha, sk, Rc[i]);
-          }
+          // r, w and s of the neighbour, one 16-byte load each
+          const float4 rc = ld_v4(Rc, col), wc = ld_v4(Wc, col);
+          const float4 sp = first ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_v4(Sp, col);
+          const float sk[3] = {first ? wc.x : fmaf(beta, sp.x, wc.x), first ? wc.y : fmaf(beta, sp.y, wc.y),
+                               first ? wc.z : fmaf(beta, sp.z, wc.z)};
+          const float x[3] = {fmaf(-alpha, sk[0], rc.x), fmaf(-alpha, sk[1], rc.y), fmaf(-alpha, sk[2], rc.z)};
           const float* v = V + 288 * j;
           y0 = fmaf(v[0], x[0], fmaf(v[32], x[1], fmaf(v[64], x[2], y0)));
           y1 = fmaf(v[96], x[0], fmaf(v[128], x[1], fmaf(v[160], x[2], y1)));
@@ -542,20 +554,27 @@ __global__ void __launch_bounds__(kPersistThreads, 1536 / kPersistThreads)
         float gam = 0.f, del = 0.f;
         if (row < A.voff[inst + 1]) {
           const float y[3] = {y0, y1, y2};
+          const float4 rc = ld_v4(Rc, row), wc = ld_v4(Wc, row);
+          const float4 sp = first ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_v4(Sp, row);
+          const float4 pp = first ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_v4(A.p32, row);
+          const float4 dd = ld_v4(A.d32, row);
+          const float R_[3] = {rc.x, rc.y, rc.z}, W_[3] = {wc.x, wc.y, wc.z}, S_[3] = {sp.x, sp.y, sp.z};
+          const float P_[3] = {pp.x, pp.y, pp.z}, D_[3] = {dd.x, dd.y, dd.z};
+          float sn[3], pn[3], dn[3], rn[3];
 #pragma unroll
           for (int k = 0; k < 3; k++) {
-            const int i = 3 * row + k;
-            const float sk = first ? Wc[i] : fmaf(beta, Sp[i], Wc[i]);
-            const float pk = first ? Rc[i] : fmaf(beta, A.p32[i], Rc[i]);
-            const float rn = fmaf(-alpha, sk, Rc[i]);
-            Sn[i] = sk;
-            A.p32[i] = pk;
-            A.d32[i] = fmaf(alpha, pk, A.d32[i]);
-            Rn[i] = rn;
-            Wn[i] = y[k];
-            gam += rn * rn;
-            del += y[k] * rn;
+            sn[k] = first ? W_[k] : fmaf(beta, S_[k], W_[k]);
+            pn[k] = first ? R_[k] : fmaf(beta, P_[k], R_[k]);
+            rn[k] = fmaf(-alpha, sn[k], R_[k]);
+            dn[k] = fmaf(alpha, pn[k], D_[k]);
+            gam += rn[k] * rn[k];
+            del += y[k] * rn[k];
           }
+          st_v4(Sn, row, sn);
+          st_v4(A.p32, row, pn);
+          st_v4(A.d32, row, dn);
+          st_v4(Rn, row, rn);
+          st_v4(Wn, row, y);
         }
         gam = warp_sum_f(gam);
         del = warp_sum_f(del);
@@ -606,7 +625,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_pw0(Arena A) {
   float y0 = 0.f, y1 = 0.f, y2 = 0.f;
   for (int j = 0; j < w; j++) {
     const int col = Cc[32 * j];
-    const float x0 = A.r32[3 * col + 0], x1 = A.r32[3 * col + 1], x2 = A.r32[3 * col + 2];
+    const float x0 = A.r32[kV * col + 0], x1 = A.r32[kV * col + 1], x2 = A.r32[kV * col + 2];
     const float* v = V + 288 * j;
     y0 = fmaf(v[0], x0, fmaf(v[32], x1, fmaf(v[64], x2, y0)));
     y1 = fmaf(v[96], x0, fmaf(v[128], x1, fmaf(v[160], x2, y1)));
@@ -617,8 +636,8 @@ __global__ void __launch_bounds__(kSliceThreads) k_mx_pw0(Arena A) {
     const float y[3] = {y0, y1, y2};
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      const float r = A.r32[3 * c.row + k];
-      A.w32[3 * c.row + k] = y[k];
+      const float r = A.r32[kV * c.row + k];
+      A.w32[kV * c.row + k] = y[k];
       gam += r * r;
       del += y[k] * r;
     }
@@ -731,7 +750,7 @@ __global__ void k_mx_correct(Arena A) {
   if (v >= A.nv) return;
   const int inst = A.vinst[v];
   if (!A.active[inst] || A.st[inst].done) return;
-  const double d0 = A.d32[3 * v], d1 = A.d32[3 * v + 1], d2 = A.d32[3 * v + 2];
+  const double d0 = A.d32[kV * v], d1 = A.d32[kV * v + 1], d2 = A.d32[kV * v + 2];
   if (A.st[inst].bjac) {
     const float* S = A.linv32 + 9 * (size_t)v;
     A.dx[3 * v + 0] += (double)S[0] * d0 + (double)S[3] * d1 + (double)S[6] * d2;
@@ -842,7 +861,12 @@ static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm
   int dev = 0, sms = 0, occ = 0;
   launch_check(cudaGetDevice(&dev), "cudaGetDevice");
   launch_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-  launch_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mx_persist<T>, T, 0),
+  // at 4 blocks of 256 threads per SM or fewer, the build with 64 registers
+  const void* kern = (const void*)k_mx_persist<T>;
+  if constexpr (T == 256) {
+    if (blocks_per_sm > 0 && blocks_per_sm <= 4) kern = (const void*)k_mx_persist<T, 4>;
+  }
+  launch_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, T, 0),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
   if (blocks_per_sm > 0) occ = std::min(occ, blocks_per_sm);
   // at least one slice per warp
@@ -853,7 +877,7 @@ static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm
   int exit1 = tail && grid2 < grid ? tail_slices : 0, resume = 0;
   void* args[] = {(void*)&A, (void*)&eta, (void*)&cap, (void*)&exit1, (void*)&resume};
   prof_begin(PK_MX_PERSIST, s);
-  launch_check(cudaLaunchCooperativeKernel((const void*)k_mx_persist<T>, dim3(grid), dim3(T), args, 0, s),
+  launch_check(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(T), args, 0, s),
                "cudaLaunchCooperativeKernel");
   prof_end(PK_MX_PERSIST, s);
   g_launches += 1;
@@ -861,7 +885,7 @@ static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm
     int exit2 = 0, resume2 = 1;
     void* args2[] = {(void*)&A, (void*)&eta, (void*)&cap, (void*)&exit2, (void*)&resume2};
     prof_begin(PK_MX_PERSIST, s);
-    launch_check(cudaLaunchCooperativeKernel((const void*)k_mx_persist<T>, dim3(grid2), dim3(T), args2, 0, s),
+    launch_check(cudaLaunchCooperativeKernel(kern, dim3(grid2), dim3(T), args2, 0, s),
                  "cudaLaunchCooperativeKernel");
     prof_end(PK_MX_PERSIST, s);
     g_launches += 1;
