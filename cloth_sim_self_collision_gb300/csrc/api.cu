@@ -261,7 +261,7 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
   A.p = m.alloc<double>(3 * (size_t)NV);
   A.z = m.alloc<double>(3 * (size_t)NV);
   A.dx = m.alloc<double>(3 * (size_t)NV);
-  CK(cudaMemsetAsync(A.z, 0, sizeof(double) * 3 * (size_t)std::max(NV, 1), s));
+  if (NV > 0) CK(cudaMemsetAsync(A.z, 0, sizeof(double) * 3 * (size_t)NV, s));
   A.part = m.alloc<double>(2 * (size_t)A.nchunk);
   {
     std::vector<long long> cb(A.nchunk, 0);
