@@ -858,39 +858,120 @@ __global__ void k_counts(Arena A, ContactBufs C) {
 // levels of the sequential sweep, one thread per cloth
 __global__ void k_token_next(Arena A) { A.ctl->token++; }
 
+// Impulse levels of each cloth's contacts, one warp per cloth.  The
+// Gauss-Seidel sweep of SelfCollisionImpulse_* (self_collision_cloth.cpp:20-212)
+// is sequential in set order; a contact's level is one more than the highest
+// level among the earlier contacts that share a vertex with it (0 if none), so
+// the contacts of a level share no vertex and each follows every earlier
+// contact it depends on: applying the levels in turn reproduces the sweep.
+// The warp takes the contacts 32 at a time in set order: a lane's in-chunk
+// predecessor for each of its 4 vertices is the last earlier lane touching it
+// (found with shuffles); a vertex without one takes the level its last
+// toucher before the chunk left in vmark (stamped with this detection's
+// token); the in-chunk levels then settle in at most 32 rounds, and for each
+// vertex the chunk's last toucher writes its level back.  The contacts are
+// then grouped by level (counts, a prefix sum, a scatter; the order within a
+// level does not matter, its contacts being independent).
 __global__ void k_impulse_levels(Arena A, ContactBufs C) {
-  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
-  if (inst >= A.ni) return;
+  const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (inst >= A.ni) return;  // the whole warp
   const int token = A.ctl->token;
-  A.st[inst].nlev = 0;
+  if (lane == 0) A.st[inst].nlev = 0;
   if (!A.active[inst]) return;
   const int lo = C.ce_inst_lo[inst], hi = C.ce_inst_hi[inst];
   if (lo >= hi) return;
+  const unsigned full = 0xffffffffu;
   int nlev = 0;
-  for (int c = lo; c < hi; c++) {
-    int l = 0;
+  for (int base = lo; base < hi; base += 32) {
+    const int c = base + lane;
+    const bool valid = c < hi;
+    int vv[4];
 #pragma unroll
-    for (int k = 1; k <= 4; k++) {
-      const int v = C.ce[5 * c + k];
-      if (C.vstamp[v] == token) l = max(l, C.vmark[v] + 1);
+    for (int k = 0; k < 4; k++) vv[k] = valid ? C.ce[5 * c + 1 + k] : -1 - 4 * lane - k;  // no match
+    int pred[4] = {-1, -1, -1, -1};
+    bool last[4] = {true, true, true, true};
+    for (int j = 0; j < 32; j++) {
+      const int u0 = __shfl_sync(full, vv[0], j), u1 = __shfl_sync(full, vv[1], j);
+      const int u2 = __shfl_sync(full, vv[2], j), u3 = __shfl_sync(full, vv[3], j);
+      if (j == lane) continue;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (vv[k] == u0 || vv[k] == u1 || vv[k] == u2 || vv[k] == u3) {
+          if (j < lane)
+            pred[k] = j;
+          else
+            last[k] = false;
+        }
+      }
+    }
+    int ext = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (valid && pred[k] < 0) {
+        const int v = vv[k];
+        if (C.vstamp[v] == token) ext = max(ext, C.vmark[v] + 1);
+      }
+    }
+    int l = ext;
+    for (int round = 0; round < 32; round++) {
+      int m = ext;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int lp = __shfl_sync(full, l, pred[k] < 0 ? lane : pred[k]);
+        if (pred[k] >= 0) m = max(m, lp + 1);
+      }
+      const bool changed = m != l;
+      l = m;
+      if (!__any_sync(full, changed)) break;
     }
 #pragma unroll
-    for (int k = 1; k <= 4; k++) {
-      const int v = C.ce[5 * c + k];
-      C.vmark[v] = l;
-      C.vstamp[v] = token;
+    for (int k = 0; k < 4; k++) {
+      if (valid && last[k]) {
+        C.vmark[vv[k]] = l;
+        C.vstamp[vv[k]] = token;
+      }
     }
-    C.level[c] = l;
-    nlev = max(nlev, l + 1);
+    if (valid) C.level[c] = l;
+    int top = valid ? l + 1 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(full, top, o));
+    nlev = max(nlev, top);
+    __syncwarp();  // the marks are read by the next chunk's lanes
   }
+  // group by level: counts at off[l + 1], prefix sums (off[l] = first of level
+  // l), a scatter that advances off[l] to the end of level l, and a shift back
   int* off = C.lev_cnt + lo + inst;  // nlev + 1 counters, disjoint per cloth
-  for (int l = 0; l <= nlev; l++) off[l] = 0;
-  for (int c = lo; c < hi; c++) off[C.level[c] + 1]++;
-  for (int l = 0; l < nlev; l++) off[l + 1] += off[l];
-  for (int c = lo; c < hi; c++) C.order[lo + off[C.level[c]]++] = c;
-  for (int l = nlev; l > 0; l--) off[l] = off[l - 1];
-  off[0] = 0;
-  A.st[inst].nlev = nlev;
+  for (int l = lane; l <= nlev; l += 32) off[l] = 0;
+  __syncwarp();
+  for (int c = lo + lane; c < hi; c += 32) atomicAdd(&off[C.level[c] + 1], 1);
+  __syncwarp();
+  int carry = 0;
+  for (int b0 = 0; b0 <= nlev; b0 += 32) {
+    const int l = b0 + lane;
+    int x = l <= nlev ? off[l] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(full, x, o);
+      if (lane >= o) x += y;
+    }
+    x += carry;
+    if (l <= nlev) off[l] = x;
+    carry = __shfl_sync(full, x, 31);
+  }
+  __syncwarp();
+  for (int c = lo + lane; c < hi; c += 32) C.order[lo + atomicAdd(&off[C.level[c]], 1)] = c;
+  __syncwarp();
+  for (int b0 = ((nlev + 31) / 32) * 32; b0 >= 0; b0 -= 32) {
+    const int l = b0 + lane;
+    const int x = (l >= 1 && l <= nlev) ? off[l - 1] : 0;
+    __syncwarp();
+    if (l >= 1 && l <= nlev) off[l] = x;
+    __syncwarp();
+  }
+  if (lane == 0) {
+    off[0] = 0;
+    A.st[inst].nlev = nlev;
+  }
 }
 
 __device__ __forceinline__ void add_v(double* v, int i, double a, double b, double c) {
@@ -1284,7 +1365,7 @@ void sort_dedupe(const Arena& A, ContactBufs& C, int n, cudaStream_t s) {
 void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, cudaStream_t s) {
   prof_begin(PK_IMPULSE, s);
   k_token_next<<<1, 1, 0, s>>>(A);
-  k_impulse_levels<<<nblk(A.ni, 32), 32, 0, s>>>(A, C);
+  k_impulse_levels<<<nblk(A.ni * 32, 128), 128, 0, s>>>(A, C);
   k_impulse_apply<<<A.ni, 128, 0, s>>>(A, C, ccd, xs, vs);
   prof_end(PK_IMPULSE, s);
   g_launches += 3;
