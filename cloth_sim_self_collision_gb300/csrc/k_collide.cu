@@ -1366,7 +1366,7 @@ void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double
   prof_begin(PK_IMPULSE, s);
   k_token_next<<<1, 1, 0, s>>>(A);
   k_impulse_levels<<<nblk(A.ni * 32, 128), 128, 0, s>>>(A, C);
-  k_impulse_apply<<<A.ni, 128, 0, s>>>(A, C, ccd, xs, vs);
+  k_impulse_apply<<<A.ni, 256, 0, s>>>(A, C, ccd, xs, vs);
   prof_end(PK_IMPULSE, s);
   g_launches += 3;
 }
