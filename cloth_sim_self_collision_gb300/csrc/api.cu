@@ -394,8 +394,8 @@ void build_arena(ArenaSet& o, const std::vector<const Cloth*>& cl, cudaStream_t 
       }
       A.slice_pbytes = m.upload(pb, s);
       A.dg_range = m.alloc<unsigned>(2 * (size_t)std::max(ni, 1));
-      A.grid_bar = m.alloc<unsigned int>(kGridBarWords);
-      CK(cudaMemsetAsync(A.grid_bar, 0, kGridBarWords * sizeof(unsigned int), s));
+      A.grid_bar = m.alloc<unsigned int>(8);
+      CK(cudaMemsetAsync(A.grid_bar, 0, 8 * sizeof(unsigned int), s));
     }
     A.mixed = 1;
   }

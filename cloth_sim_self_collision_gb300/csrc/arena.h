@@ -76,10 +76,6 @@ constexpr int kOverflowZone = 2;     // impact-zone members beyond the padded so
 constexpr int kOverflowBuffers = 4;  // leaf pairs, test queues or candidates beyond their buffers
 constexpr int kOverflowSolver = 8;   // refinement cycles beyond the graph's cap, or a barrier gave up
 
-// words of the persistent solver's grid barrier: 8 control words, then one
-// arrival counter per group of 32 blocks (grids of up to 4096 blocks)
-constexpr int kGridBarWords = 8 + 128;
-
 struct FrameCtl {
   int ccd_pass;     // CCD passes run in this frame
   int riz_pass;     // impact-zone passes run
@@ -171,9 +167,8 @@ struct Arena {
   // per cloth: smallest and largest diagonal entry of the assembled matrix (as
   // the bits of positive floats) for the choice of preconditioner
   unsigned* dg_range = nullptr;
-  unsigned int* grid_bar = nullptr; // [0] group arrivals, [1] generation, [2] gave up, [3] cloths still
-                                    // iterating, [4] last iteration of a launch that left for the tail
-                                    // launch, [8 + g] arrivals of the 32 blocks of group g
+  unsigned int* grid_bar = nullptr; // [0] arrivals, [1] generation, [2] gave up, [3] cloths still iterating,
+                                    // [4] last iteration of a launch that left for the tail launch
   FrameCtl* ctl = nullptr;          // frame control on the device
   int dev_grid = 0;                 // blocks of the grid-stride narrow-phase kernels of a graph frame
   int narrow_regs = 0;              // 128: FP64 narrow-phase kernels capped at 128 registers

@@ -336,27 +336,11 @@ __device__ bool grid_sync(const Arena& A) {
     const unsigned gen = bar[1];
     // with the test hook set, block 0 does not arrive and every wait runs out
     const bool hold = A.bar_hold != 0 && blockIdx.x == 0;
-    // arrival in two levels, so no single counter takes every block's atomic:
-    // a block counts in its group of 32; the group's last block counts in
-    // [0]; the last group's last block resets [0] and advances the generation
-    // (each counter is reset before the generation moves, so before any block
-    // can arrive at the next barrier)
-    bool flipped = false;
-    if (!hold) {
-      const unsigned g = blockIdx.x >> 5, groups = (gridDim.x + 31) >> 5;
-      const unsigned members = min(32u, gridDim.x - (g << 5));
-      if (atomicAdd(&A.grid_bar[8 + g], 1u) == members - 1) {
-        atomicExch(&A.grid_bar[8 + g], 0u);
-        __threadfence();
-        if (atomicAdd(&A.grid_bar[0], 1u) == groups - 1) {
-          atomicExch(&A.grid_bar[0], 0u);
-          __threadfence();
-          atomicAdd(&A.grid_bar[1], 1u);
-          flipped = true;
-        }
-      }
-    }
-    if (!flipped) {
+    if (!hold && atomicAdd(&A.grid_bar[0], 1u) == gridDim.x - 1) {
+      atomicExch(&A.grid_bar[0], 0u);
+      __threadfence();
+      atomicAdd(&A.grid_bar[1], 1u);
+    } else {
       // poll with a pause of A.bar_sleep_ns between reads; give up (flag the
       // error for every block) after A.bar_timeout_ns of the device's clock
       const unsigned long long t0 = global_ns();
@@ -887,7 +871,6 @@ static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm
   if (blocks_per_sm > 0) occ = std::min(occ, blocks_per_sm);
   // at least one slice per warp
   const int grid = std::max(1, std::min((A.nslice + T / 32 - 1) / (T / 32), sms * std::max(occ, 1)));
-  if (grid > 32 * (kGridBarWords - 8)) throw CudaError("persistent solver: grid larger than its barrier's groups");
   // the tail launch: one warp for each of at most tail_slices slices
   const bool tail = tail_slices > 0 && A.ni <= kRebalanceMax;
   const int grid2 = std::max(1, std::min(grid, (tail_slices + T / 32 - 1) / (T / 32)));
@@ -911,7 +894,7 @@ static void persist_launch(const Arena& A, float eta, int cap, int blocks_per_sm
 
 void launch_mx_inner_persistent(const Arena& A, float eta, int cap, int blocks_per_sm, int threads, int tail_slices,
                                 cudaStream_t s) {
-  launch_check(cudaMemsetAsync(A.grid_bar, 0, kGridBarWords * sizeof(unsigned int), s), "cudaMemsetAsync");
+  launch_check(cudaMemsetAsync(A.grid_bar, 0, 8 * sizeof(unsigned int), s), "cudaMemsetAsync");
   launch_check(cudaMemsetAsync(A.red_cnt, 0, sizeof(int) * (size_t)std::max(A.ni, 1), s), "cudaMemsetAsync");
   const int blocks = (A.nslice * 32 + kSliceThreads - 1) / kSliceThreads;
   k_mx_inner_init<<<blocks, kSliceThreads, 0, s>>>(A);
