@@ -382,17 +382,11 @@ __device__ __forceinline__ void count_fp64_test(const Arena& A, int slot) {
 // apart).  Pass 2: the FP64 tests run on
 // the packed queues, one kind per kernel, so their warps stay full.  The
 // candidates' order does not matter (they are sorted afterwards).
-__device__ __forceinline__ void enqueue(const ContactBufs& C, int kind, int pid, int test) {
-  const int slot = warp_append(&C.counters[6 + kind]);
-  if ((unsigned)slot >= (unsigned)C.q_cap[kind]) {
-    C.counters[3] = 1;
-    return;
-  }
-  C.queue[kind][slot] = make_int2(pid, test);
-}
-
+// Pass 1 for leaf pair pid: the tests that survive the FP32 prefilters, as
+// bit masks (face-vertex tests 0-5, edge-edge tests 6-14 as bits 0-8)
 __device__ __forceinline__ void narrow_filter_pair(const Arena& A, const ContactBufs& C, int ccd,
-                                                   double delta_override, int pid) {
+                                                   double delta_override, int pid, unsigned& fvm,
+                                                   unsigned& eem) {
   // the 9 edge pairs of a triangle pair (kEE), as compile-time indices
   constexpr int kE[9][4] = {{0, 1, 0, 1}, {0, 1, 1, 2}, {0, 1, 2, 0}, {1, 2, 0, 1}, {1, 2, 1, 2},
                             {1, 2, 2, 0}, {2, 0, 0, 1}, {2, 0, 1, 2}, {2, 0, 2, 0}};
@@ -445,7 +439,7 @@ __device__ __forceinline__ void narrow_filter_pair(const Arena& A, const Contact
       const int* f = on_a ? va : vb;
       if (q == f[0] || q == f[1] || q == f[2]) continue;
       if (!overlap32(on_a ? fa : fb, on_a ? bb[k] : ba[k])) continue;
-      enqueue(C, 0, pid, test);
+      fvm |= 1u << test;
     }
   }
 #pragma unroll
@@ -477,21 +471,74 @@ __device__ __forceinline__ void narrow_filter_pair(const Arena& A, const Contact
       }
       if (keep && ee_prx_reject32(a0, a1, b0, b1, du)) keep = false;
     }
-    if (keep) enqueue(C, 1, pid, 6 + k);
+    if (keep) eem |= 1u << k;
+  }
+}
+
+// The survivors of a warp's 32 leaf pairs into the two test queues: one atomic
+// per queue and warp (a scan of the lanes' counts gives each lane its slots).
+// Every lane of the warp calls it; the queue order does not matter (the
+// contact set is sorted by key afterwards).
+__device__ __forceinline__ void enqueue_masks(const ContactBufs& C, int pid, unsigned fvm, unsigned eem) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int nf = __popc(fvm), ne = __popc(eem);
+  int sf = nf, se = ne;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int yf = __shfl_up_sync(full, sf, o), ye = __shfl_up_sync(full, se, o);
+    if (lane >= o) {
+      sf += yf;
+      se += ye;
+    }
+  }
+  const int tf = __shfl_sync(full, sf, 31), te = __shfl_sync(full, se, 31);
+  int bf = 0, be = 0;
+  if (lane == 0) {
+    if (tf) bf = atomicAdd(&C.counters[6], tf);
+    if (te) be = atomicAdd(&C.counters[7], te);
+  }
+  bf = __shfl_sync(full, bf, 0);
+  be = __shfl_sync(full, be, 0);
+  int of = bf + sf - nf, oe = be + se - ne;
+  while (fvm) {
+    const int t = __ffs(fvm) - 1;
+    fvm &= fvm - 1;
+    if ((unsigned)of < (unsigned)C.q_cap[0])
+      C.queue[0][of] = make_int2(pid, t);
+    else
+      C.counters[3] = 1;
+    of++;
+  }
+  while (eem) {
+    const int t = __ffs(eem) - 1;
+    eem &= eem - 1;
+    if ((unsigned)oe < (unsigned)C.q_cap[1])
+      C.queue[1][oe] = make_int2(pid, 6 + t);
+    else
+      C.counters[3] = 1;
+    oe++;
   }
 }
 
 __global__ void __launch_bounds__(kT) k_narrow_filter(Arena A, ContactBufs C, int ccd, double delta_override,
                                                       int npairs) {
   const int pid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pid < npairs) narrow_filter_pair(A, C, ccd, delta_override, pid);
+  unsigned fvm = 0, eem = 0;
+  if (pid < npairs) narrow_filter_pair(A, C, ccd, delta_override, pid, fvm, eem);
+  enqueue_masks(C, pid, fvm, eem);
 }
 
-// the same over the pair count the broad phase left on the device (grid-stride)
+// the same over the pair count the broad phase left on the device (grid-stride,
+// the loop uniform over each block so that whole warps enqueue together)
 __global__ void __launch_bounds__(kT) k_narrow_filter_dev(Arena A, ContactBufs C, int ccd, double delta_override) {
   const int n = min(__ldcg(&C.counters[0]), C.pair_cap);
-  for (int pid = blockIdx.x * blockDim.x + threadIdx.x; pid < n; pid += gridDim.x * blockDim.x)
-    narrow_filter_pair(A, C, ccd, delta_override, pid);
+  for (int b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+    const int pid = b + threadIdx.x;
+    unsigned fvm = 0, eem = 0;
+    if (pid < n) narrow_filter_pair(A, C, ccd, delta_override, pid, fvm, eem);
+    enqueue_masks(C, pid, fvm, eem);
+  }
 }
 
 // pass 2, face-vertex tests (grid-stride over their queue)
