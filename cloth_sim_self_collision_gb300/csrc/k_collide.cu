@@ -198,6 +198,30 @@ __device__ __forceinline__ void load_box32(const float* src, float* b) {
   }
 }
 
+// Leaf pairs a thread of the broad phase found, appended to C.pairs in batches
+// of 8 (one atomic per batch; the pair order does not matter, the contact set
+// being sorted by key afterwards).  A count past the capacity sets the overflow
+// flag, and the host regrows the buffer from the count.
+struct PairBuf {
+  int2 p[8];
+  int n;
+};
+__device__ __forceinline__ void pairbuf_flush(const ContactBufs& C, PairBuf& b) {
+  if (b.n == 0) return;
+  const int slot = atomicAdd(&C.counters[0], b.n);
+  for (int i = 0; i < b.n; i++) {
+    if ((unsigned)(slot + i) < (unsigned)C.pair_cap)
+      C.pairs[slot + i] = b.p[i];
+    else
+      C.counters[3] = 1;
+  }
+  b.n = 0;
+}
+__device__ __forceinline__ void pairbuf_add(const ContactBufs& C, PairBuf& b, int2 pr) {
+  b.p[b.n++] = pr;
+  if (b.n == 8) pairbuf_flush(C, b);
+}
+
 __device__ __forceinline__ void traverse_tri(const Arena& A, const ContactBufs& C, int t) {
   const int inst = A.tinst[t];
   if (!A.active[inst] || A.st[inst].diverged) return;
@@ -209,6 +233,8 @@ __device__ __forceinline__ void traverse_tri(const Arena& A, const ContactBufs& 
   int k = A.preoff[inst];
   const int end = A.preoff[inst + 1];
   int found = 0;
+  PairBuf buf;
+  buf.n = 0;
   while (k < end) {
     const int n = A.pre[k];
     float nb32[6];
@@ -224,18 +250,16 @@ __device__ __forceinline__ void traverse_tri(const Arena& A, const ContactBufs& 
       }
       if (++found > kMaxPairsPerTriangle) {
         A.st[inst].diverged = 1;
+        pairbuf_flush(C, buf);
         return;
       }
-      const int slot = warp_append(&C.counters[0]);
-      if ((unsigned)slot < (unsigned)C.pair_cap)
-        C.pairs[slot] = make_int2(la, n);
-      else
-        C.counters[3] = 1;
+      pairbuf_add(C, buf, make_int2(la, n));
       k = A.skip[k];
     } else {
       k++;
     }
   }
+  pairbuf_flush(C, buf);
 }
 
 __global__ void k_traverse(Arena A, ContactBufs C) {
@@ -258,6 +282,8 @@ __device__ __forceinline__ void traverse_dirty_tri(const Arena& A, const Contact
   int k = A.preoff[inst];
   const int end = A.preoff[inst + 1];
   int found = 0;
+  PairBuf buf;
+  buf.n = 0;
   while (k < end) {
     const int n = A.pre[k];
     float nb32[6];
@@ -273,22 +299,18 @@ __device__ __forceinline__ void traverse_dirty_tri(const Arena& A, const Contact
       }
       if (++found > 2 * kMaxPairsPerTriangle) {
         A.st[inst].diverged = 1;
+        pairbuf_flush(C, buf);
         return;
       }
       const int ob = A.leaf_lo[n];
       const bool other_dirty = A.tdirty[A.node[3 * n + 1]] != 0;
-      if (n != la && (!other_dirty || oa < ob)) {
-        const int slot = warp_append(&C.counters[0]);
-        if ((unsigned)slot < (unsigned)C.pair_cap)
-          C.pairs[slot] = (oa < ob) ? make_int2(la, n) : make_int2(n, la);
-        else
-          C.counters[3] = 1;
-      }
+      if (n != la && (!other_dirty || oa < ob)) pairbuf_add(C, buf, (oa < ob) ? make_int2(la, n) : make_int2(n, la));
       k = A.skip[k];
     } else {
       k++;
     }
   }
+  pairbuf_flush(C, buf);
 }
 
 __global__ void k_traverse_dirty(Arena A, ContactBufs C) {
