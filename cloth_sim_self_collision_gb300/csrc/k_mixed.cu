@@ -539,7 +539,9 @@ __global__ void __launch_bounds__(kPersistThreads, kMinBlocks)
         float y0 = 0.f, y1 = 0.f, y2 = 0.f;
 #pragma unroll 2
         for (int j = 0; j < w; j++) {
-          const int col = Cc[32 * j];
+          // the matrix streams (read once per iteration, evict first), so that
+          // the gathered vectors keep their place in L2
+          const int col = __ldcs(Cc + 32 * j);
           // r, w and s of the neighbour, one 16-byte load each
           const float4 rc = ld_v4(Rc, col), wc = ld_v4(Wc, col);
           const float4 sp = first ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_v4(Sp, col);
@@ -547,9 +549,9 @@ __global__ void __launch_bounds__(kPersistThreads, kMinBlocks)
                                first ? wc.z : fmaf(beta, sp.z, wc.z)};
           const float x[3] = {fmaf(-alpha, sk[0], rc.x), fmaf(-alpha, sk[1], rc.y), fmaf(-alpha, sk[2], rc.z)};
           const float* v = V + 288 * j;
-          y0 = fmaf(v[0], x[0], fmaf(v[32], x[1], fmaf(v[64], x[2], y0)));
-          y1 = fmaf(v[96], x[0], fmaf(v[128], x[1], fmaf(v[160], x[2], y1)));
-          y2 = fmaf(v[192], x[0], fmaf(v[224], x[1], fmaf(v[256], x[2], y2)));
+          y0 = fmaf(__ldcs(v), x[0], fmaf(__ldcs(v + 32), x[1], fmaf(__ldcs(v + 64), x[2], y0)));
+          y1 = fmaf(__ldcs(v + 96), x[0], fmaf(__ldcs(v + 128), x[1], fmaf(__ldcs(v + 160), x[2], y1)));
+          y2 = fmaf(__ldcs(v + 192), x[0], fmaf(__ldcs(v + 224), x[1], fmaf(__ldcs(v + 256), x[2], y2)));
         }
         float gam = 0.f, del = 0.f;
         if (row < A.voff[inst + 1]) {
