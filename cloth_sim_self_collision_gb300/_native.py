@@ -49,7 +49,7 @@ EXPORTS = [
 class CsTuneResult(ctypes.Structure):
     _fields_ = [("mx_blocks_per_sm", ctypes.c_int), ("mx_tail_slices", ctypes.c_int),
                 ("graph_grid_per_sm", ctypes.c_int), ("narrow_regs", ctypes.c_int),
-                ("bar_sleep_ns", ctypes.c_int), ("frame_ms", ctypes.c_double),
+                ("bar_sleep_ns", ctypes.c_int), ("impulse_cluster", ctypes.c_int), ("frame_ms", ctypes.c_double),
                 ("candidates", ctypes.c_int),
                 ("cached", ctypes.c_int)]
 

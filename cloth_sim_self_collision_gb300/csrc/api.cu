@@ -412,6 +412,7 @@ void install(cs_ctx* c, ArenaSet& o) {
   graph_release(c);
   o.A.narrow_regs = c->narrow_regs;
   o.A.bar_sleep_ns = c->bar_sleep_ns;
+  o.A.impulse_cluster = c->impulse_cluster;
   o.A.mx_eta_big = c->mx_eta_big;
   o.A.bar_timeout_ns = c->bar_timeout_ns;
   o.A.bar_hold = c->bar_hold;
@@ -1003,6 +1004,7 @@ int cs_create(int device, int precision, cs_ctx** out) {
   // contexts made by the library itself (the serving loop) take the frame mode from here
   if (const char* e = std::getenv("CLOTHGPU_FRAME_MODE")) c->graph_mode = std::strcmp(e, "host") != 0;
   if (const char* e = std::getenv("CLOTHGPU_BAR_SLEEP_NS")) c->bar_sleep_ns = std::max(0, std::atoi(e));
+  if (const char* e = std::getenv("CLOTHGPU_IMPULSE_CLUSTER")) c->impulse_cluster = std::atoi(e) == 8 ? 8 : 1;
   // failure-detection tests: a short barrier time-out, and a barrier that
   // block 0 never reaches (every wait then runs out and the frame fails with
   // CS_ERR_CUDA, the context staying usable)
@@ -1010,6 +1012,7 @@ int cs_create(int device, int precision, cs_ctx** out) {
   if (const char* e = std::getenv("CLOTHGPU_BAR_HOLD")) c->bar_hold = std::atoi(e) != 0;
   c->A.narrow_regs = c->narrow_regs;
   c->A.bar_sleep_ns = c->bar_sleep_ns;
+  c->A.impulse_cluster = c->impulse_cluster;
   c->A.mx_eta_big = c->mx_eta_big;
   c->A.bar_timeout_ns = c->bar_timeout_ns;
   c->A.bar_hold = c->bar_hold;
@@ -1660,6 +1663,8 @@ void apply_tune(cs_ctx* c, const cs_tune_result& r) {
   c->A.narrow_regs = r.narrow_regs;
   c->bar_sleep_ns = r.bar_sleep_ns;
   c->A.bar_sleep_ns = r.bar_sleep_ns;
+  c->impulse_cluster = r.impulse_cluster;
+  c->A.impulse_cluster = r.impulse_cluster;
   graph_release(c);
 }
 }  // namespace
@@ -1729,6 +1734,7 @@ int cs_autotune(cs_ctx* c, int frames, cs_tune_result* out) {
     best.graph_grid_per_sm = c->graph_grid_per_sm;
     best.narrow_regs = c->narrow_regs;
     best.bar_sleep_ns = c->bar_sleep_ns;
+    best.impulse_cluster = c->impulse_cluster;
     time_cfg(best);  // untimed warm pass: contact buffers grow to these frames' needs
     best.frame_ms = time_cfg(best);
     // coordinate descent over the three shapes
@@ -1751,6 +1757,7 @@ int cs_autotune(cs_ctx* c, int frames, cs_tune_result* out) {
     if (c->graph_mode) try_values(&cs_tune_result::graph_grid_per_sm, {4, 8, 16});
     try_values(&cs_tune_result::narrow_regs, {0, 128});
     if (c->precision == CS_PREC_MIXED) try_values(&cs_tune_result::bar_sleep_ns, {256, 64, 0});
+    try_values(&cs_tune_result::impulse_cluster, {1, 8});
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     best.candidates = timed;

@@ -173,6 +173,7 @@ struct Arena {
   int dev_grid = 0;                 // blocks of the grid-stride narrow-phase kernels of a graph frame
   int narrow_regs = 0;              // 128: FP64 narrow-phase kernels capped at 128 registers
   int bar_sleep_ns = 256;           // pause between polls of a waiting grid barrier
+  int impulse_cluster = 1;          // blocks (one cluster) sweeping a cloth's impulse levels
   float mx_eta_big = 1.0e-4f;       // FP32 inner tolerance of large cloths (mixed solve)
   long long bar_timeout_ns = 2000000000;  // a waiting grid barrier gives up after this long
   int bar_hold = 0;                 // test hook: block 0 never arrives at the grid barrier

@@ -117,6 +117,7 @@ struct cs_ctx {
   // pause between polls of the persistent solver's grid barrier (ns), its
   // time-out, and the test hook that keeps block 0 from arriving
   int bar_sleep_ns = 256;
+  int impulse_cluster = 1;  // blocks per cloth of the impulse sweep (a cluster when > 1)
   long long bar_timeout_ns = 2000000000;
   int bar_hold = 0;
   // inner FP32 solve of a refinement cycle: relative residual target and cap

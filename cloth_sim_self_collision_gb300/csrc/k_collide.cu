@@ -22,6 +22,8 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <cooperative_groups.h>
+
 #include "cert.cuh"
 #include "kernels.h"
 
@@ -1132,6 +1134,28 @@ __device__ void impulse_one(const DevParams& P, const int* e, const double* x, d
 }
 
 // one CTA per cloth applies its levels in order
+// The same sweep by a cluster of blocks per cloth (cloth = cluster index): a
+// level's contacts spread over the cluster's SMs, whose FP64 pipes then work
+// together, and the levels are separated by cluster barriers.
+__global__ void k_impulse_apply_cluster(Arena A, ContactBufs C, int ccd, const double* xs, double* vs) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank(), size = (int)cl.num_blocks();
+  const int inst = blockIdx.x / size;
+  if (inst >= A.ni || !A.active[inst]) return;  // the whole cluster
+  const int nlev = A.st[inst].nlev;
+  if (nlev == 0) return;
+  const int lo = C.ce_inst_lo[inst];
+  const int* off = C.lev_cnt + lo + inst;
+  const DevParams& P = A.prm[inst];
+  const int stride = size * blockDim.x;
+  for (int l = 0; l < nlev; l++) {
+    for (int j = off[l] + rank * blockDim.x + threadIdx.x; j < off[l + 1]; j += stride)
+      impulse_one(P, C.ce + 5 * C.order[lo + j], xs, vs, ccd);
+    cl.sync();
+  }
+}
+
 __global__ void k_impulse_apply(Arena A, ContactBufs C, int ccd, const double* xs, double* vs) {
   const int inst = blockIdx.x;
   if (!A.active[inst]) return;
@@ -1435,7 +1459,23 @@ void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double
   prof_begin(PK_IMPULSE, s);
   k_token_next<<<1, 1, 0, s>>>(A);
   k_impulse_levels<<<nblk(A.ni * 32, 128), 128, 0, s>>>(A, C);
-  k_impulse_apply<<<A.ni, 256, 0, s>>>(A, C, ccd, xs, vs);
+  if (A.impulse_cluster > 1) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(A.ni * A.impulse_cluster));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)A.impulse_cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    launch_check(cudaLaunchKernelEx(&cfg, k_impulse_apply_cluster, A, C, ccd, xs, vs), "cudaLaunchKernelEx");
+  } else {
+    k_impulse_apply<<<A.ni, 256, 0, s>>>(A, C, ccd, xs, vs);
+  }
   prof_end(PK_IMPULSE, s);
   g_launches += 3;
 }

@@ -363,8 +363,9 @@ int cs_frame_overflows(cs_ctx *ctx, long long reasons[4]);
  * for candidate launch shapes (coordinate descent over the persistent solver's
  * blocks per SM, the slice count below which it continues in a smaller tail
  * launch, the blocks per SM of the narrow-phase kernels of graph frames,
- * whether the FP64 narrow-phase kernels are capped at 128 registers, and the
- * pause between polls of the persistent solver's grid barrier),
+ * whether the FP64 narrow-phase kernels are capped at 128 registers, the
+ * pause between polls of the persistent solver's grid barrier, and the blocks
+ * per cloth of the impulse sweep),
  * restoring the state after each, and keeps the fastest.  The frames do not
  * depend on these shapes, so the simulation continues exactly where it was.
  * Results are cached per arena shape (cloths, vertices, slices, precision) for
@@ -375,6 +376,7 @@ typedef struct cs_tune_result {
   int graph_grid_per_sm;  /* graph frames: narrow-phase blocks per SM           */
   int narrow_regs;        /* FP64 narrow-phase kernels: 0 free, 128 capped       */
   int bar_sleep_ns;       /* persistent solver: pause between barrier polls (ns) */
+  int impulse_cluster;    /* impulse sweep: blocks per cloth (1, or a cluster of 8) */
   double frame_ms;        /* measured time of a frame with these shapes         */
   int candidates;         /* configurations timed                               */
   int cached;             /* 1: taken from an earlier call on the same shape    */

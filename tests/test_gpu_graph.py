@@ -95,6 +95,18 @@ def test_narrow_register_variants_equal(monkeypatch):
     assert sum(sum(s["n_ccd"]) > 0 for fr in b[1] for s in fr) > 0
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_impulse_cluster_sweep_equal(monkeypatch, graph):
+    """The impulse sweep by a cluster of 8 blocks per cloth (a variant the
+    autotuner may pick) gives the same frames bit for bit, through contact."""
+    cl = scene.config_batch(count=16)
+    a = run(cl, "mixed", graph, 40)
+    monkeypatch.setenv("CLOTHGPU_IMPULSE_CLUSTER", "8")
+    b = run(cl, "mixed", graph, 40)
+    assert same(a, b)
+    assert sum(s["impulse_applied"] > 0 for fr in b[1] for s in fr) > 0
+
+
 def test_autotune_leaves_frames_unchanged():
     """cs_autotune times candidate launch shapes on frames from the current state
     and restores it: the frames that follow equal those of an untuned context
@@ -124,4 +136,4 @@ def test_autotune_leaves_frames_unchanged():
     assert t0["cached"] == 0 and t0["candidates"] >= 3 and t0["frame_ms"] > 0
     assert t1["cached"] == 1 and t1["mx_blocks_per_sm"] == t0["mx_blocks_per_sm"]
     assert t0["mx_blocks_per_sm"] in (4, 5, 6) and t0["graph_grid_per_sm"] in (4, 8, 16)
-    assert t0["narrow_regs"] in (0, 128)
+    assert t0["narrow_regs"] in (0, 128) and t0["impulse_cluster"] in (1, 8)
