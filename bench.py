@@ -563,6 +563,17 @@ def native(args):
             line[f"batched_{prec}"] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
                                        "p50_step_ms": r["p50_step_ms"], "p99_step_ms": r["p99_step_ms"],
                                        "kernel_ms": {k: [round(v[0], 3), v[1]] for k, v in r["prof"].items() if v[1]}}
+            # the FP64 SpMV of the FP64 path: its device-counted algorithmic bytes over
+            # its time, as a fraction of HBM (it is bound by the FP64 pipe: the row's
+            # blocks are added in the reference's order on one lane)
+            ms64, n64 = r["prof"].get("cg_spmv", (0.0, 0))
+            b64 = r["counts"].get("spmv64_bytes", 0)
+            if ms64 > 0 and b64 > 0:
+                ach = b64 / (ms64 / 1e3) / 1e9
+                line[f"batched_{prec}"]["roofline_cg_spmv"] = {
+                    "kernel": "cg_spmv", "bound": "fp64 pipe", "launches": n64,
+                    "bytes_per_launch": b64 / max(n64, 1), "achieved": ach, "unit": "GB/s",
+                    "hbm_frac": ach / peaks["hbm_gbs"]}
     if plain is not None:
         line["plain_gpu_fp64_one_per_launch"] = plain
         line["vs_plain_gpu"] = head["value"] / plain["value"]
