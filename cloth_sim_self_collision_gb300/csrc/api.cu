@@ -45,9 +45,7 @@ void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t
   C.cand_cap = cand_cap;
   C.ce_cap = cand_cap;
   C.pairs = m.alloc<int2>(pair_cap);
-  // face-vertex tests: up to 6 a pair, as many as the edge-edge queue's 9 in
-  // the contact-rich frames, so the same default (a regrow costs a graph frame)
-  C.q_cap[0] = q_fv > 0 ? q_fv : (int)std::min<long long>(2LL * pair_cap, 0x7fffffffLL);
+  C.q_cap[0] = q_fv > 0 ? q_fv : std::max(pair_cap / 2, 4096);
   C.q_cap[1] = q_ee > 0 ? q_ee : (int)std::min<long long>(2LL * pair_cap, 0x7fffffffLL);
   C.queue[0] = m.alloc<int2>(C.q_cap[0]);
   C.queue[1] = m.alloc<int2>(C.q_cap[1]);
@@ -954,9 +952,9 @@ size_t cloth_device_bytes(const ClothTopo& t) {
   const size_t sell = ((np + 31) / 32) * 32 * 16;  // SELL entries, padded to the slice width
   b += sell * (36 + 4) + (nb + np) * 8;        // FP32 values, columns, SELL positions
   b += np * (36 + 10 * 16);                    // FP32 diagonal inverse and the 10 solver vectors (16 B each)
-  // pairs, the two test queues and the two queues of the certificates' piece
-  // stage (2 pair capacities each), and the candidate buffers
-  b += (16 * nt + 4096) * 8 * 9 + (4 * nt + 4096) * 120;
+  // pairs, the test queues and the queues of the certificates' piece stage
+  // (face-vertex half a pair capacity, edge-edge two), and the candidate buffers
+  b += (16 * nt + 4096) * 8 * 6 + (4 * nt + 4096) * 120;
   b += np * (2 * 4 + 2 * 8 + 72);              // vertex marks, zone keys and sums
   b += np * 48;                                // FP32 hi/lo positions and displacements
   return b + (1 << 16);
