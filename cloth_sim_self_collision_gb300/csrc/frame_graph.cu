@@ -353,7 +353,7 @@ void graph_capture(cs_ctx* c) {
   Arena& A = c->A;
   for (int k = 0; k < 2; k++)
     if (!c->gstream[k]) CK(cudaStreamCreateWithFlags(&c->gstream[k], cudaStreamNonBlocking));
-  // padded sort sizes: eight times the largest counts the frames so far saw
+  // padded sort sizes: four times the largest counts the frames so far saw
   // (contacts grow as cloths settle into contact, and a frame that outgrows
   // the graph costs a graph frame, a host-driven frame and a capture, far more
   // than sorting padded keys), at least CLOTHGPU_GRAPH_SORT_MIN candidates and
@@ -361,8 +361,8 @@ void graph_capture(cs_ctx* c) {
   // frames outgrow their sizes)
   const char* es = std::getenv("CLOTHGPU_GRAPH_SORT_MIN");
   const char* ez = std::getenv("CLOTHGPU_GRAPH_ZONE_MIN");
-  const long long smin = es ? std::max(1LL, std::atoll(es)) : 131072, zmin = ez ? std::max(1LL, std::atoll(ez)) : 32768;
-  const long long smul = es ? 2 : 8, zmul = ez ? 2 : 8;
+  const long long smin = es ? std::max(1LL, std::atoll(es)) : 65536, zmin = ez ? std::max(1LL, std::atoll(ez)) : 16384;
+  const long long smul = es ? 2 : 4, zmul = ez ? 2 : 4;
   c->g_scand = std::min(c->C.cand_cap, pow2_at_least(std::max<long long>(smul * c->max_ncand, smin)));
   c->g_szone = std::min(A.nv, pow2_at_least(std::max<long long>(zmul * c->max_zone, zmin)));
   {
