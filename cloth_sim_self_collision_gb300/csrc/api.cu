@@ -63,6 +63,7 @@ void alloc_contacts_into(const Arena& A, ContactBufs& C, DevMem& m, cudaStream_t
   C.counters = m.alloc<int>(16);
   C.level = m.alloc<int>(cand_cap);
   C.order = m.alloc<int>(cand_cap);
+  C.imp_pre = m.alloc<double>(9 * (size_t)cand_cap);
   C.lev_cnt = m.alloc<int>((size_t)cand_cap + A.ni + 1);
   C.vmark = m.alloc<int>(A.nv);
   C.vstamp = m.alloc<int>(A.nv);
@@ -954,7 +955,7 @@ size_t cloth_device_bytes(const ClothTopo& t) {
   b += np * (36 + 10 * 16);                    // FP32 diagonal inverse and the 10 solver vectors (16 B each)
   // pairs, the test queues and the queues of the certificates' piece stage
   // (face-vertex half a pair capacity, edge-edge two), and the candidate buffers
-  b += (16 * nt + 4096) * 8 * 6 + (4 * nt + 4096) * 120;
+  b += (16 * nt + 4096) * 8 * 6 + (4 * nt + 4096) * 192;
   b += np * (2 * 4 + 2 * 8 + 72);              // vertex marks, zone keys and sums
   b += np * 48;                                // FP32 hi/lo positions and displacements
   return b + (1 << 16);
@@ -1475,6 +1476,7 @@ static void contacts_in(cs_ctx* c, int i, const int* ce, int n) {
   hi[i] = n;
   CK(cudaMemcpyAsync(c->C.ce_inst_lo, lo.data(), sizeof(int) * lo.size(), cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->C.ce_inst_hi, hi.data(), sizeof(int) * hi.size(), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->C.counters + 2, &n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
 }
 

@@ -206,6 +206,7 @@ struct ContactBufs {
                               // certificates' piece stage, [12] / [13] CCD tests left to FP64
   int* level = nullptr;       // impulse level per contact
   int* order = nullptr;       // contacts grouped by level
+  double* imp_pre = nullptr;  // per contact: position-only terms of the proximity impulse (9)
   int* lev_cnt = nullptr;     // per cloth: level count (then offsets)
   int* vmark = nullptr;       // per vertex: last level touching it (stamped)
   int* vstamp = nullptr;

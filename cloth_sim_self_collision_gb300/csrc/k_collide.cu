@@ -943,7 +943,7 @@ __global__ void k_token_next(Arena A) { A.ctl->token++; }
 // vertex the chunk's last toucher writes its level back.  The contacts are
 // then grouped by level (counts, a prefix sum, a scatter; the order within a
 // level does not matter, its contacts being independent).
-__global__ void k_impulse_levels(Arena A, ContactBufs C) {
+__global__ void k_impulse_levels(Arena A, ContactBufs C, int ccd) {
   const int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (inst >= A.ni) return;  // the whole warp
   const int token = A.ctl->token;
@@ -956,9 +956,12 @@ __global__ void k_impulse_levels(Arena A, ContactBufs C) {
   for (int base = lo; base < hi; base += 32) {
     const int c = base + lane;
     const bool valid = c < hi;
+    // a proximity contact that the positions alone reject changes no velocity:
+    // it depends on nothing and nothing depends on it (level 0)
+    const bool live = valid && (ccd || C.imp_pre[9 * (size_t)c + 8] != 0.0);
     int vv[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) vv[k] = valid ? C.ce[5 * c + 1 + k] : -1 - 4 * lane - k;  // no match
+    for (int k = 0; k < 4; k++) vv[k] = live ? C.ce[5 * c + 1 + k] : -1 - 4 * lane - k;  // no match
     int pred[4] = {-1, -1, -1, -1};
     bool last[4] = {true, true, true, true};
     for (int j = 0; j < 32; j++) {
@@ -978,7 +981,7 @@ __global__ void k_impulse_levels(Arena A, ContactBufs C) {
     int ext = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      if (valid && pred[k] < 0) {
+      if (live && pred[k] < 0) {
         const int v = vv[k];
         if (C.vstamp[v] == token) ext = max(ext, C.vmark[v] + 1);
       }
@@ -997,7 +1000,7 @@ __global__ void k_impulse_levels(Arena A, ContactBufs C) {
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      if (valid && last[k]) {
+      if (live && last[k]) {
         C.vmark[vv[k]] = l;
         C.vstamp[vv[k]] = token;
       }
@@ -1051,22 +1054,112 @@ __device__ __forceinline__ void add_v(double* v, int i, double a, double b, doub
   v[3 * i + 2] += c;
 }
 
-// one contact of the sweep (SelfCollisionImpulse_Proximity / _CCD)
-__device__ void impulse_one(const DevParams& P, const int* e, const double* x, double* v, int ccd) {
-  const double delta = P.contact_clearance, stiff = P.stiff_contact, dt = P.dt, mass = P.mass_point;
+// Position-only terms of one proximity impulse (SelfCollisionImpulse_Proximity,
+// self_collision_cloth.cpp:20-112), computed for every contact in parallel
+// before the sweep, in q: the barycentric weights (w0 w1 w2, or w01 w23), the
+// normal, the threshold 0.1 depth / dt, the elastic impulse dt stiff depth and
+// the weight denominator.  A contact that the positions alone reject (weights
+// outside [0, 1], distance above the clearance) gets a zero denominator: it
+// changes no velocity and leaves the sweep's dependency chain.
+__device__ void prox_prep(const DevParams& P, const int* e, const double* x, double* q) {
+  const double delta = P.contact_clearance, stiff = P.stiff_contact, dt = P.dt;
+  const int i0 = e[1], i1 = e[2], i2 = e[3], i3 = e[4];
+  const V3<double> p0 = ld3(x, i0), p1 = ld3(x, i1), p2 = ld3(x, i2), p3 = ld3(x, i3);
+  q[8] = 0.0;
+  if (e[0]) {  // face (i0 i1 i2) - vertex i3
+    double w0, w1;
+    const double dist = dist_face_vertex(p0, p1, p2, p3, w0, w1);
+    if (w0 < 0 || w0 > 1) return;
+    if (w1 < 0 || w1 > 1) return;
+    if (dist > delta) return;
+    const double w2 = 1.0 - w0 - w1;
+    const V3<double> pc = w0 * p0 + w1 * p1 + w2 * p2;
+    const V3<double> nrm = normalized(p3 - pc);
+    const double depth = delta - dot(p3 - pc, nrm);
+    q[0] = w0;
+    q[1] = w1;
+    q[2] = w2;
+    q[3] = nrm.x;
+    q[4] = nrm.y;
+    q[5] = nrm.z;
+    q[6] = 0.1 * depth / dt;
+    q[7] = dt * stiff * depth;
+    q[8] = 1 + w0 * w0 + w1 * w1 + w2 * w2;
+  } else {  // edge (i0 i1) - edge (i2 i3)
+    double w01, w23;
+    const double dist = dist_edge_edge(p0, p1, p2, p3, w01, w23);
+    if (w01 < 0 || w01 > 1) return;
+    if (w23 < 0 || w23 > 1) return;
+    if (dist > delta) return;
+    const V3<double> c01 = (1 - w01) * p0 + w01 * p1;
+    const V3<double> c23 = (1 - w23) * p2 + w23 * p3;
+    const V3<double> nrm = normalized(c23 - c01);
+    const double depth = delta - length(c23 - c01);
+    q[0] = w01;
+    q[1] = w23;
+    q[2] = 0.0;
+    q[3] = nrm.x;
+    q[4] = nrm.y;
+    q[5] = nrm.z;
+    q[6] = 0.1 * depth / dt;
+    q[7] = dt * stiff * depth;
+    q[8] = w01 * w01 + (1 - w01) * (1 - w01) + w23 * w23 + (1 - w23) * (1 - w23);
+  }
+}
+
+// the velocity part of one proximity impulse, from the terms of prox_prep
+__device__ void impulse_prx(const DevParams& P, const int* e, const double* q, double* v) {
+  const double den = q[8];
+  if (den == 0.0) return;
+  const double mass = P.mass_point;
+  const int i0 = e[1], i1 = e[2], i2 = e[3], i3 = e[4];
+  const V3<double> v0 = ld3((const double*)v, i0), v1 = ld3((const double*)v, i1), v2 = ld3((const double*)v, i2),
+                   v3 = ld3((const double*)v, i3);
+  const V3<double> nrm = mk<double>(q[3], q[4], q[5]);
+  const double thr = q[6], imp_el = q[7];
+  if (e[0]) {  // face (i0 i1 i2) - vertex i3
+    const double w0 = q[0], w1 = q[1], w2 = q[2];
+    const double rel_v = dot(v3 - w0 * v0 - w1 * v1 - w2 * v2, nrm);
+    if (rel_v > thr) return;
+    const double imp_ie = mass * (thr - rel_v);
+    const double imp_min = (imp_el < imp_ie) ? imp_el : imp_ie;
+    double imp_mod = 2 * imp_min / den;
+    imp_mod /= mass;
+    imp_mod *= 0.25;
+    const double mx = -nrm.x, my = -nrm.y, mz = -nrm.z;
+    add_v(v, i0, mx * imp_mod * w0, my * imp_mod * w0, mz * imp_mod * w0);
+    add_v(v, i1, mx * imp_mod * w1, my * imp_mod * w1, mz * imp_mod * w1);
+    add_v(v, i2, mx * imp_mod * w2, my * imp_mod * w2, mz * imp_mod * w2);
+    add_v(v, i3, nrm.x * imp_mod, nrm.y * imp_mod, nrm.z * imp_mod);
+  } else {  // edge (i0 i1) - edge (i2 i3)
+    const double w01 = q[0], w23 = q[1];
+    const double rel_v = dot((1 - w23) * v2 + w23 * v3 - (1 - w01) * v0 - w01 * v1, nrm);
+    if (rel_v > thr) return;
+    const double imp_ie = mass * (thr - rel_v);
+    const double imp_min = (imp_el < imp_ie) ? imp_el : imp_ie;
+    double imp_mod = 2 * imp_min / den;
+    imp_mod /= mass;
+    imp_mod *= 0.25;
+    const double mx = -nrm.x, my = -nrm.y, mz = -nrm.z;
+    add_v(v, i0, mx * imp_mod * (1 - w01), my * imp_mod * (1 - w01), mz * imp_mod * (1 - w01));
+    add_v(v, i1, mx * imp_mod * w01, my * imp_mod * w01, mz * imp_mod * w01);
+    add_v(v, i2, nrm.x * imp_mod * (1 - w23), nrm.y * imp_mod * (1 - w23), nrm.z * imp_mod * (1 - w23));
+    add_v(v, i3, nrm.x * imp_mod * w23, nrm.y * imp_mod * w23, nrm.z * imp_mod * w23);
+  }
+}
+
+// one contact of the CCD sweep (SelfCollisionImpulse_CCD, self_collision_cloth.cpp:116-212)
+__device__ void impulse_ccd(const DevParams& P, const int* e, const double* x, double* v) {
+  const double delta = P.contact_clearance, dt = P.dt, mass = P.mass_point;
   const int i0 = e[1], i1 = e[2], i2 = e[3], i3 = e[4];
   const V3<double> p0 = ld3(x, i0), p1 = ld3(x, i1), p2 = ld3(x, i2), p3 = ld3(x, i3);
   const V3<double> v0 = ld3((const double*)v, i0), v1 = ld3((const double*)v, i1), v2 = ld3((const double*)v, i2),
                    v3 = ld3((const double*)v, i3);
-  double t = 0;
-  if (ccd) {
-    t = coplanar_time(p0, p1, p2, p3, p0 + v0, p1 + v1, p2 + v2, p3 + v3);
-    if (t < 0 || t > 1) return;
-  }
+  const double t = coplanar_time(p0, p1, p2, p3, p0 + v0, p1 + v1, p2 + v2, p3 + v3);
+  if (t < 0 || t > 1) return;
   if (e[0]) {  // face (i0 i1 i2) - vertex i3
     double w0, w1;
-    const double dist = ccd ? dist_face_vertex(p0 + t * v0, p1 + t * v1, p2 + t * v2, p3 + t * v3, w0, w1)
-                            : dist_face_vertex(p0, p1, p2, p3, w0, w1);
+    const double dist = dist_face_vertex(p0 + t * v0, p1 + t * v1, p2 + t * v2, p3 + t * v3, w0, w1);
     if (w0 < 0 || w0 > 1) return;
     if (w1 < 0 || w1 > 1) return;
     if (dist > delta) return;
@@ -1074,23 +1167,11 @@ __device__ void impulse_one(const DevParams& P, const int* e, const double* x, d
     const V3<double> pc = w0 * p0 + w1 * p1 + w2 * p2;
     const V3<double> nrm = normalized(p3 - pc);
     const double rel_v = dot(v3 - w0 * v0 - w1 * v1 - w2 * v2, nrm);
-    double imp_mod;
-    if (!ccd) {
-      const double depth = delta - dot(p3 - pc, nrm);
-      if (rel_v > 0.1 * depth / dt) return;
-      const double imp_el = dt * stiff * depth;
-      const double imp_ie = mass * (0.1 * depth / dt - rel_v);
-      const double imp_min = (imp_el < imp_ie) ? imp_el : imp_ie;
-      imp_mod = 2 * imp_min / (1 + w0 * w0 + w1 * w1 + w2 * w2);
-      imp_mod /= mass;
-      imp_mod *= 0.25;
-    } else {
-      if (rel_v > 0.1 * delta / dt) return;
-      const double imp = mass * (0.1 * delta / dt - rel_v);
-      imp_mod = 2 * imp / (1.0 + w0 * w0 + w1 * w1 + w2 * w2);
-      imp_mod /= mass;
-      imp_mod *= 0.1;
-    }
+    if (rel_v > 0.1 * delta / dt) return;
+    const double imp = mass * (0.1 * delta / dt - rel_v);
+    double imp_mod = 2 * imp / (1.0 + w0 * w0 + w1 * w1 + w2 * w2);
+    imp_mod /= mass;
+    imp_mod *= 0.1;
     const double mx = -nrm.x, my = -nrm.y, mz = -nrm.z;
     add_v(v, i0, mx * imp_mod * w0, my * imp_mod * w0, mz * imp_mod * w0);
     add_v(v, i1, mx * imp_mod * w1, my * imp_mod * w1, mz * imp_mod * w1);
@@ -1098,8 +1179,7 @@ __device__ void impulse_one(const DevParams& P, const int* e, const double* x, d
     add_v(v, i3, nrm.x * imp_mod, nrm.y * imp_mod, nrm.z * imp_mod);
   } else {  // edge (i0 i1) - edge (i2 i3)
     double w01, w23;
-    const double dist = ccd ? dist_edge_edge(p0 + t * v0, p1 + t * v1, p2 + t * v2, p3 + t * v3, w01, w23)
-                            : dist_edge_edge(p0, p1, p2, p3, w01, w23);
+    const double dist = dist_edge_edge(p0 + t * v0, p1 + t * v1, p2 + t * v2, p3 + t * v3, w01, w23);
     if (w01 < 0 || w01 > 1) return;
     if (w23 < 0 || w23 > 1) return;
     if (dist > delta) return;
@@ -1108,28 +1188,34 @@ __device__ void impulse_one(const DevParams& P, const int* e, const double* x, d
     const V3<double> nrm = normalized(c23 - c01);
     const double rel_v = dot((1 - w23) * v2 + w23 * v3 - (1 - w01) * v0 - w01 * v1, nrm);
     const double wsum = w01 * w01 + (1 - w01) * (1 - w01) + w23 * w23 + (1 - w23) * (1 - w23);
-    double imp_mod;
-    if (!ccd) {
-      const double depth = delta - length(c23 - c01);
-      if (rel_v > 0.1 * depth / dt) return;
-      const double imp_el = dt * stiff * depth;
-      const double imp_ie = mass * (0.1 * depth / dt - rel_v);
-      const double imp_min = (imp_el < imp_ie) ? imp_el : imp_ie;
-      imp_mod = 2 * imp_min / wsum;
-      imp_mod /= mass;
-      imp_mod *= 0.25;
-    } else {
-      if (rel_v > 0.1 * delta / dt) return;
-      const double imp = mass * (0.1 * delta / dt - rel_v);
-      imp_mod = 2 * imp / wsum;
-      imp_mod /= mass;
-      imp_mod *= 0.1;
-    }
+    if (rel_v > 0.1 * delta / dt) return;
+    const double imp = mass * (0.1 * delta / dt - rel_v);
+    double imp_mod = 2 * imp / wsum;
+    imp_mod /= mass;
+    imp_mod *= 0.1;
     const double mx = -nrm.x, my = -nrm.y, mz = -nrm.z;
     add_v(v, i0, mx * imp_mod * (1 - w01), my * imp_mod * (1 - w01), mz * imp_mod * (1 - w01));
     add_v(v, i1, mx * imp_mod * w01, my * imp_mod * w01, mz * imp_mod * w01);
     add_v(v, i2, nrm.x * imp_mod * (1 - w23), nrm.y * imp_mod * (1 - w23), nrm.z * imp_mod * (1 - w23));
     add_v(v, i3, nrm.x * imp_mod * w23, nrm.y * imp_mod * w23, nrm.z * imp_mod * w23);
+  }
+}
+
+// contact c of the sweep
+__device__ __forceinline__ void impulse_at(const DevParams& P, const ContactBufs& C, int c, const double* xs,
+                                           double* vs, int ccd) {
+  if (ccd)
+    impulse_ccd(P, C.ce + 5 * c, xs, vs);
+  else
+    impulse_prx(P, C.ce + 5 * c, C.imp_pre + 9 * (size_t)c, vs);
+}
+
+// prox_prep for every contact of the list, C.counters[2] of them
+__global__ void k_impulse_prep(Arena A, ContactBufs C, const double* xs) {
+  const int n = C.counters[2];
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const int* e = C.ce + 5 * c;
+    prox_prep(A.prm[A.vinst[e[1]]], e, xs, C.imp_pre + 9 * (size_t)c);
   }
 }
 
@@ -1151,7 +1237,7 @@ __global__ void k_impulse_apply_cluster(Arena A, ContactBufs C, int ccd, const d
   const int stride = size * blockDim.x;
   for (int l = 0; l < nlev; l++) {
     for (int j = off[l] + rank * blockDim.x + threadIdx.x; j < off[l + 1]; j += stride)
-      impulse_one(P, C.ce + 5 * C.order[lo + j], xs, vs, ccd);
+      impulse_at(P, C, C.order[lo + j], xs, vs, ccd);
     cl.sync();
   }
 }
@@ -1166,7 +1252,7 @@ __global__ void k_impulse_apply(Arena A, ContactBufs C, int ccd, const double* x
   const DevParams& P = A.prm[inst];
   for (int l = 0; l < nlev; l++) {
     for (int j = off[l] + threadIdx.x; j < off[l + 1]; j += blockDim.x)
-      impulse_one(P, C.ce + 5 * C.order[lo + j], xs, vs, ccd);
+      impulse_at(P, C, C.order[lo + j], xs, vs, ccd);
     __syncthreads();
   }
 }
@@ -1457,8 +1543,19 @@ void sort_dedupe(const Arena& A, ContactBufs& C, int n, cudaStream_t s) {
 
 void launch_impulses(const Arena& A, const ContactBufs& C, int ccd, const double* xs, double* vs, cudaStream_t s) {
   prof_begin(PK_IMPULSE, s);
+  if (!ccd) {
+    static int grid = 0;
+    if (grid == 0) {
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      grid = 4 * (sms > 0 ? sms : 1);
+    }
+    k_impulse_prep<<<grid, 128, 0, s>>>(A, C, xs);
+    g_launches++;
+  }
   k_token_next<<<1, 1, 0, s>>>(A);
-  k_impulse_levels<<<nblk(A.ni * 32, 128), 128, 0, s>>>(A, C);
+  k_impulse_levels<<<nblk(A.ni * 32, 128), 128, 0, s>>>(A, C, ccd);
   if (A.impulse_cluster > 1) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(A.ni * A.impulse_cluster));
